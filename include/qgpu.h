@@ -1,0 +1,151 @@
+/*
+ * qgpu.h — C ABI of libquantr_gpu, the GB300 (sm_103a) state-vector engine behind
+ * quantr's `Circuit::simulate` / `SimulatedCircuit::{get_state, measure_all}`.
+ *
+ * quantr (Rust crate 0.6.0) has no FFI of its own: the path it replaces is the crate-private
+ * call chain `Circuit::simulate` (src/circuit.rs:364-388) -> `simulate_with_register`
+ * (src/circuit/simulation.rs:21-57) -> `apply_gate` (src/circuit/simulation.rs:64-135), then
+ * `SimulatedCircuit::measure_all` (src/simulated_circuit.rs:63-73) -> `SuperPosition::measure`
+ * (src/circuit/states/super_positions.rs:332-342). Each entry point below names the reference
+ * item it stands in for. A host binding (Rust `extern "C"` block, C++ `quantr.hpp`, Python
+ * ctypes) lowers quantr's flat gate list into `qgpu_op` records and calls these functions.
+ *
+ * Conventions
+ *  - Every function returns an `int` status: QGPU_OK (0) or a negative QGPU_ERR_* code.
+ *    `qgpu_last_error()` returns a thread-local message for the last failure on this thread.
+ *  - Amplitudes cross the boundary as interleaved (re, im) doubles, index i = sum over wires w
+ *    of bit_w << (n-1-w): wire 0 is the most significant bit, as in quantr's
+ *    `ProductState::binary_basis` (src/circuit/states/product_states.rs:205-215).
+ *  - A handle owns one device state vector and one CUDA stream. Handles are not thread-safe;
+ *    different handles may be driven from different threads. All calls are stream-ordered and
+ *    synchronise before returning host-visible results.
+ *  - No call falls back to a CPU implementation: a missing or failing device is an error.
+ */
+#ifndef QGPU_H
+#define QGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+#define QGPU_OK               0
+#define QGPU_ERR_INVALID     -1  /* bad argument: wire out of range, overlapping wires, size */
+#define QGPU_ERR_OOM         -2  /* device allocation failed (e.g. 35 qubits of complex128)  */
+#define QGPU_ERR_CUDA        -3  /* a CUDA runtime call or kernel launch failed               */
+#define QGPU_ERR_TIMEOUT     -4  /* a bounded device-side wait ran out                        */
+#define QGPU_ERR_UNSUPPORTED -5  /* valid request this build does not serve                  */
+#define QGPU_ERR_NONUNITARY  -6  /* adjoint gradient asked for a circuit with Custom gates   */
+
+/* ---- precision of the device state ----------------------------------------------------- */
+#define QGPU_C128 0   /* complex128: quantr's `Complex64` amplitudes (num-complex f64 pairs) */
+#define QGPU_C64  1   /* complex64: float pairs; reductions (norm, probabilities) stay in f64 */
+
+/* ---- arithmetic mode for complex128 ------------------------------------------------------
+ * QGPU_MODE_EXACT  one pass per gate, f64 products and sums without contraction, in the
+ *                  reference's accumulation order (simulation.rs:168-179): amplitudes equal
+ *                  the reference's value for value.
+ * QGPU_MODE_FAST   gate fusion and GB300 kernels; f64 arithmetic carried on the FP32/INT
+ *                  pipes as unevaluated float pairs (GB300 issues f64 at ~1/64 of the FP32
+ *                  rate). Results stay within 1e-12 max-abs of the reference.
+ * QGPU_MODE_F64    same fusion as FAST but native f64 FMA arithmetic (for comparison).       */
+#define QGPU_MODE_FAST  0
+#define QGPU_MODE_EXACT 1
+#define QGPU_MODE_F64   2
+
+/* ---- gate kinds: one per `quantr::Gate` variant (src/circuit/gate.rs:19-106) ---------- */
+enum qgpu_gate_kind {
+    QGPU_GATE_ID = 0,
+    QGPU_GATE_H, QGPU_GATE_X, QGPU_GATE_Y, QGPU_GATE_Z,
+    QGPU_GATE_S, QGPU_GATE_SDAG, QGPU_GATE_T, QGPU_GATE_TDAG,
+    QGPU_GATE_RX, QGPU_GATE_RY, QGPU_GATE_RZ,
+    QGPU_GATE_X90, QGPU_GATE_Y90, QGPU_GATE_MX90, QGPU_GATE_MY90,
+    QGPU_GATE_PHASE,
+    QGPU_GATE_CR, QGPU_GATE_CRK, QGPU_GATE_CZ, QGPU_GATE_CY, QGPU_GATE_CNOT, QGPU_GATE_SWAP,
+    QGPU_GATE_TOFFOLI,
+    QGPU_GATE_CUSTOM,
+    QGPU_GATE_COUNT
+};
+
+/* Largest number of wires one Custom gate may act on (controls + target). The host tabulates
+ * a Custom gate into a dense 2^k x 2^k block, so k = 10 is a 16 MiB matrix. */
+#define QGPU_MAX_OP_WIRES 10
+
+/* One non-identity gate of quantr's flat column list, in simulation order. `target` is the
+ * gate's wire (`gate_pos = counter % num_qubits`, simulation.rs:43). `controls` hold the wires
+ * of the variant's usize fields in declaration order: CNot/CY/CZ/Swap/CR/CRk -> [c],
+ * Toffoli(c1, c2) -> [c1, c2], Custom(_, controls, _) -> controls. The gate then acts on the
+ * local register [controls..., target], first entry most significant (simulation.rs:96-112).
+ *
+ * Custom gates (simulation.rs:102-105, 137-156): the host evaluates the user function on
+ * each of the 2^k local basis states j and stores the image as column j of a column-major
+ * 2^k x 2^k complex matrix at mats[mat_offset ...] (interleaved re, im: entry (l, j) at
+ * mats[mat_offset + 2*(j*2^k + l)]), and none_flags[none_offset + j] = 1 where the function
+ * returned `None`. Non-unitary blocks are allowed. */
+typedef struct qgpu_op {
+    int32_t kind;                          /* enum qgpu_gate_kind                        */
+    int32_t target;                        /* wire of the gate                           */
+    int32_t n_controls;                    /* used entries of controls[]                 */
+    int32_t k;                             /* CRk's integer k                            */
+    int32_t controls[QGPU_MAX_OP_WIRES];   /* control wires in variant order             */
+    double  param;                         /* angle of Rx/Ry/Rz/Phase/CR                  */
+    int64_t mat_offset;                    /* Custom: offset (in doubles) into mats       */
+    int64_t none_offset;                   /* Custom: offset (in bytes) into none_flags   */
+} qgpu_op;
+
+typedef struct qgpu_handle qgpu_handle;
+
+/* ---- lifetime --------------------------------------------------------------------------- */
+
+/* Allocates a 2^n_qubits state on the current CUDA device, set to |0...0>.
+ * Replaces `SuperPosition::new_unchecked` (src/circuit/states/super_positions_unchecked.rs:39-46).
+ * precision: QGPU_C128 or QGPU_C64. Fails with QGPU_ERR_OOM when the state does not fit. */
+int qgpu_create(int n_qubits, int precision, qgpu_handle** out);
+int qgpu_destroy(qgpu_handle* h);
+int qgpu_num_qubits(const qgpu_handle* h);
+int qgpu_set_mode(qgpu_handle* h, int mode);             /* QGPU_MODE_*                  */
+const char* qgpu_last_error(void);                        /* thread-local, never NULL     */
+
+/* ---- register in / out ------------------------------------------------------------------ */
+
+/* |0...0>: the default register of `Circuit::simulate` (circuit.rs:376-378). */
+int qgpu_set_zero(qgpu_handle* h);
+/* `Circuit::change_register` (circuit.rs:463-473): len must equal 2^n amplitudes. */
+int qgpu_upload(qgpu_handle* h, const double* interleaved, size_t n_amplitudes);
+/* `SimulatedCircuit::get_state` / `take_state` (src/simulated_circuit.rs:158-160, 185-187). */
+int qgpu_download(qgpu_handle* h, double* interleaved_out, size_t n_amplitudes);
+
+/* ---- simulation ------------------------------------------------------------------------- */
+
+/* Applies ops[0..n_ops) in order: the loop of `simulate_with_register` (simulation.rs:37-56)
+ * with one `apply_gate` (simulation.rs:64-135) per op. Identity ops are skipped. */
+int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
+                       const double* mats, size_t n_mat_doubles,
+                       const uint8_t* none_flags, size_t n_none_flags);
+
+/* ---- measurement ------------------------------------------------------------------------ */
+
+/* `SimulatedCircuit::measure_all(shots)` (simulated_circuit.rs:63-73): `shots` draws of
+ * `SuperPosition::measure` (super_positions.rs:332-342) from a seeded counter-based generator.
+ * Each shot returns the first index i with u < sum_{j<=i} |a_j|^2, or fails (`None`) when u is
+ * at least the total. The histogram comes back sorted by index: idx_out[0..*n_unique) and
+ * cnt_out[0..*n_unique); `cap` is the capacity of both arrays. *n_failed counts `None` shots. */
+int qgpu_measure(qgpu_handle* h, uint64_t shots, uint64_t seed,
+                 uint64_t* idx_out, uint64_t* cnt_out, size_t cap,
+                 size_t* n_unique, uint64_t* n_failed);
+
+/* The same sampling rule for caller-supplied uniforms u[0..n) in [0, 1): out[i] is the index
+ * drawn for u[i], or -1 for `None`. Used to check the sampler shot by shot. */
+int qgpu_measure_uniforms(qgpu_handle* h, const double* u, size_t n, int64_t* out);
+
+/* f64 reductions of the state: sum |a_i|^2, and the amplitude checksum sum a_i. */
+int qgpu_norm(qgpu_handle* h, double* out);
+int qgpu_checksum(qgpu_handle* h, double* re_out, double* im_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QGPU_H */

@@ -1,0 +1,617 @@
+// plan.cpp — gate tabulation (the reference's formulas) and the fast-path pass planner.
+#include "plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace qgpu {
+
+int fail(int code, const std::string& msg);  // state.cu
+
+namespace {
+
+const double FRAC_1_SQRT_2 = 0.70710678118654752440;  // std::f64::consts::FRAC_1_SQRT_2
+const double PI = 3.14159265358979323846;             // std::f64::consts::PI
+
+// exp(i x) as num-complex computes it: from_polar(exp(0) = 1, x) = (1*cos x, 1*sin x).
+cd expi(double x) { return cd(1.0 * std::cos(x), 1.0 * std::sin(x)); }
+
+// 2x2 column images of the single-wire gates, standard_gate_ops.rs:37-182.
+// c0 = image of |0>, c1 = image of |1>.
+void one_qubit_images(const qgpu_op& op, cd c0[2], cd c1[2]) {
+    const double a = op.param;
+    const cd O(0.0, 0.0);
+    switch (op.kind) {
+        case QGPU_GATE_H:
+            c0[0] = cd(FRAC_1_SQRT_2, 0); c0[1] = cd(FRAC_1_SQRT_2, 0);
+            c1[0] = cd(FRAC_1_SQRT_2, 0); c1[1] = cd(-FRAC_1_SQRT_2, 0);
+            break;
+        case QGPU_GATE_RX: {
+            const cd c(std::cos(0.5 * a), 0), s(0, -std::sin(0.5 * a));
+            c0[0] = c; c0[1] = s; c1[0] = s; c1[1] = c;
+            break;
+        }
+        case QGPU_GATE_RY: {
+            const cd c(std::cos(0.5 * a), 0), sp(std::sin(0.5 * a), 0), sn(-std::sin(0.5 * a), 0);
+            c0[0] = c; c0[1] = sp; c1[0] = sn; c1[1] = c;
+            break;
+        }
+        case QGPU_GATE_RZ:
+            c0[0] = expi((-a) * 0.5); c0[1] = O; c1[0] = O; c1[1] = expi(a * 0.5);
+            break;
+        case QGPU_GATE_PHASE: {  // global phase exp(i a/2) * I
+            const cd e = expi(a * 0.5);
+            c0[0] = e; c0[1] = O; c1[0] = O; c1[1] = e;
+            break;
+        }
+        case QGPU_GATE_X90:
+            c0[0] = O; c0[1] = cd(0, -1); c1[0] = cd(0, -1); c1[1] = O;
+            break;
+        case QGPU_GATE_Y90:
+            c0[0] = O; c0[1] = cd(-1, 0); c1[0] = cd(1, 0); c1[1] = O;
+            break;
+        case QGPU_GATE_MX90:
+            c0[0] = O; c0[1] = cd(0, 1); c1[0] = cd(0, 1); c1[1] = O;
+            break;
+        case QGPU_GATE_MY90:
+            c0[0] = O; c0[1] = cd(1, 0); c1[0] = cd(-1, 0); c1[1] = O;
+            break;
+        case QGPU_GATE_T:
+            c0[0] = cd(1, 0); c0[1] = O; c1[0] = O; c1[1] = cd(FRAC_1_SQRT_2, FRAC_1_SQRT_2);
+            break;
+        case QGPU_GATE_TDAG:
+            c0[0] = cd(1, 0); c0[1] = O; c1[0] = O; c1[1] = cd(FRAC_1_SQRT_2, -FRAC_1_SQRT_2);
+            break;
+        case QGPU_GATE_S:
+            c0[0] = cd(1, 0); c0[1] = O; c1[0] = O; c1[1] = cd(0, 1);
+            break;
+        case QGPU_GATE_SDAG:
+            c0[0] = cd(1, 0); c0[1] = O; c1[0] = O; c1[1] = cd(0, -1);
+            break;
+        case QGPU_GATE_X:
+            c0[0] = O; c0[1] = cd(1, 0); c1[0] = cd(1, 0); c1[1] = O;
+            break;
+        case QGPU_GATE_Y:
+            c0[0] = O; c0[1] = cd(0, 1); c1[0] = cd(0, -1); c1[1] = O;
+            break;
+        case QGPU_GATE_Z:
+        default:
+            c0[0] = cd(1, 0); c0[1] = O; c1[0] = O; c1[1] = cd(-1, 0);
+            break;
+    }
+}
+
+bool is_one_qubit(int kind) { return kind >= QGPU_GATE_H && kind <= QGPU_GATE_PHASE; }
+
+}  // namespace
+
+int op_arity(const qgpu_op& op, int n, int* k_out) {
+    int k = 1;
+    switch (op.kind) {
+        case QGPU_GATE_CR: case QGPU_GATE_CRK: case QGPU_GATE_CZ: case QGPU_GATE_CY:
+        case QGPU_GATE_CNOT: case QGPU_GATE_SWAP:
+            k = 2;
+            break;
+        case QGPU_GATE_TOFFOLI:
+            k = 3;
+            break;
+        case QGPU_GATE_CUSTOM:
+            if (op.n_controls < 0 || op.n_controls >= QGPU_MAX_OP_WIRES)
+                return fail(QGPU_ERR_INVALID, "Custom gate with " + std::to_string(op.n_controls) +
+                                                  " controls: at most " +
+                                                  std::to_string(QGPU_MAX_OP_WIRES - 1) + " supported");
+            k = op.n_controls + 1;
+            break;
+        default:
+            if (!is_one_qubit(op.kind))
+                return fail(QGPU_ERR_INVALID, "unknown gate kind " + std::to_string(op.kind));
+    }
+    if (op.kind != QGPU_GATE_CUSTOM && op.n_controls != k - 1)
+        return fail(QGPU_ERR_INVALID, "gate kind " + std::to_string(op.kind) + " takes " +
+                                          std::to_string(k - 1) + " control(s), got " +
+                                          std::to_string(op.n_controls));
+    int wires[QGPU_MAX_OP_WIRES];
+    for (int m = 0; m < k - 1; ++m) wires[m] = op.controls[m];
+    wires[k - 1] = op.target;
+    for (int m = 0; m < k; ++m) {
+        // circuit.rs:157-166 / 284-288: positions and control nodes must lie on the register.
+        if (wires[m] < 0 || wires[m] >= n)
+            return fail(QGPU_ERR_INVALID, "The position, " + std::to_string(wires[m]) +
+                                              ", is out of bounds for the circuit with " +
+                                              std::to_string(n) + " qubits.");
+        for (int m2 = 0; m2 < m; ++m2)
+            if (wires[m] == wires[m2])  // circuit.rs:276-283
+                return fail(QGPU_ERR_INVALID, "The gate has overlapping control nodes or a control "
+                                              "node that equals the gate's position " +
+                                                  std::to_string(wires[m]) + ".");
+    }
+    *k_out = k;
+    return QGPU_OK;
+}
+
+int tabulate(const qgpu_op& op, int n, const double* mats, size_t n_mats, const uint8_t* none,
+             size_t n_none, LocalGate* out) {
+    int k = 0;
+    int st = op_arity(op, n, &k);
+    if (st != QGPU_OK) return st;
+    out->k = k;
+    for (int m = 0; m < k - 1; ++m) out->wires[m] = op.controls[m];
+    out->wires[k - 1] = op.target;
+    const size_t d = (size_t)1 << k;
+    out->M.assign(d * d, cd(0, 0));
+    out->none.assign(d, 0);
+    auto M = [&](size_t j, size_t l) -> cd& { return out->M[j * d + l]; };
+    if (is_one_qubit(op.kind)) {
+        cd c0[2], c1[2];
+        one_qubit_images(op, c0, c1);
+        M(0, 0) = c0[0]; M(0, 1) = c0[1]; M(1, 0) = c1[0]; M(1, 1) = c1[1];
+        return QGPU_OK;
+    }
+    switch (op.kind) {
+        case QGPU_GATE_CNOT:  // standard_gate_ops.rs:189-196
+            M(0, 0) = 1; M(1, 1) = 1; M(2, 3) = 1; M(3, 2) = 1;
+            return QGPU_OK;
+        case QGPU_GATE_CY:  // :199-206
+            M(0, 0) = 1; M(1, 1) = 1; M(2, 3) = cd(0, 1); M(3, 2) = cd(0, -1);
+            return QGPU_OK;
+        case QGPU_GATE_CZ:  // :209-216
+            M(0, 0) = 1; M(1, 1) = 1; M(2, 2) = 1; M(3, 3) = -1;
+            return QGPU_OK;
+        case QGPU_GATE_SWAP:  // :219-226
+            M(0, 0) = 1; M(1, 2) = 1; M(2, 1) = 1; M(3, 3) = 1;
+            return QGPU_OK;
+        case QGPU_GATE_CR:    // :229-237
+        case QGPU_GATE_CRK: {  // :240-249, angle (2*pi)/2^k
+            M(0, 0) = 1; M(1, 1) = 1; M(2, 2) = 1;
+            const double ang = op.kind == QGPU_GATE_CR ? op.param
+                                                       : (2.0 * PI) / std::pow(2.0, (double)op.k);
+            M(3, 3) = expi(ang);
+            return QGPU_OK;
+        }
+        case QGPU_GATE_TOFFOLI:  // :256-267
+            for (size_t j = 0; j < 8; ++j) M(j, j == 6 ? 7 : j == 7 ? 6 : j) = 1;
+            return QGPU_OK;
+        case QGPU_GATE_CUSTOM: {
+            if (!mats || !none || op.mat_offset < 0 || op.none_offset < 0 ||
+                (size_t)op.mat_offset + 2 * d * d > n_mats || (size_t)op.none_offset + d > n_none)
+                return fail(QGPU_ERR_INVALID, "Custom gate table lies outside mats/none_flags");
+            const double* src = mats + op.mat_offset;
+            for (size_t j = 0; j < d; ++j) {
+                out->none[j] = none[op.none_offset + j] ? 1 : 0;
+                for (size_t l = 0; l < d; ++l)
+                    M(j, l) = cd(src[2 * (j * d + l)], src[2 * (j * d + l) + 1]);
+            }
+            return QGPU_OK;
+        }
+        default:
+            return fail(QGPU_ERR_INVALID, "unknown gate kind " + std::to_string(op.kind));
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Planner
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+// A gate reduced to "controlled 2x2 on one bit" form, a swap of two bits, or a generic block.
+struct AGate {
+    enum Kind { ONE, SWAP, BLOCK } kind;
+    int t = 0;          // target bit (full index)
+    uint64_t cm = 0;    // control bits that must be 1
+    cd u[2][2];         // u[out][in]
+    int a = 0, b = 0;   // SWAP bits
+    int block = -1;     // BLOCK: index into plan.customs
+    uint64_t support = 0;  // all bits the gate reads or writes
+};
+
+int unit_code(cd x) {
+    if (x == cd(1, 0)) return 0;
+    if (x == cd(0, 1)) return 1;
+    if (x == cd(-1, 0)) return 2;
+    if (x == cd(0, -1)) return 3;
+    return -1;
+}
+bool is_zero(cd x) { return x.real() == 0.0 && x.imag() == 0.0; }
+
+void put_ff(float* dst, cd x) {
+    const float rh = (float)x.real();
+    const float rl = (float)(x.real() - (double)rh);
+    const float ih = (float)x.imag();
+    const float il = (float)(x.imag() - (double)ih);
+    dst[0] = rh; dst[1] = rl; dst[2] = ih; dst[3] = il;
+}
+
+DevStep blank_step(uint8_t type) {
+    DevStep s;
+    std::memset(&s, 0, sizeof(s));
+    s.type = type;
+    return s;
+}
+
+void set_entry(DevStep& s, int slot, cd x) {
+    put_ff(s.ff + 4 * slot, x);
+    s.d[2 * slot] = x.real();
+    s.d[2 * slot + 1] = x.imag();
+}
+
+// Host-side step with its full-index bit(s) still unresolved to tile positions.
+struct HStep {
+    DevStep s;
+    int need[2] = {-1, -1};  // full-index bits that must be tile bits
+    bool diagonal = false;
+    bool unit = false;       // no arithmetic
+    // diagonal bookkeeping (PHASE/DIAG) for table fusion
+    uint64_t dcm = 0;        // bits that must be 1
+    int dfb = -1;            // DIAG: selecting bit
+    cd d0 = 1, d1 = 1;       // DIAG entries; PHASE uses d1
+};
+
+int popcount64(uint64_t x) { return __builtin_popcountll(x); }
+
+int step_cost(const HStep& h, int policy) {
+    const DevStep& s = h.s;
+    const int pc = popcount64(s.cm);
+    const bool ff = policy == POL_FF;
+    switch (s.type) {
+        case ST_DENSE: return ff ? 95 : 8;
+        case ST_REAL: return ff ? 45 : 4;
+        case ST_PERM: return 2;
+        case ST_SWAP: return 0;
+        case ST_PHASE: return h.unit ? 3 : ((ff ? 45 : 4) >> std::min(pc, 4)) + 2;
+        case ST_DIAG: return h.unit ? 4 : (ff ? 48 : 5);
+        case ST_TABLE: return ((ff ? 55 : 8) * s.nfields >> std::min(pc, 4)) + 4;
+    }
+    return 0;
+}
+
+// Steps for a controlled 2x2 u on bit t under control mask cm.
+void emit_one(const AGate& g, std::vector<HStep>& out) {
+    const cd u00 = g.u[0][0], u01 = g.u[0][1], u10 = g.u[1][0], u11 = g.u[1][1];
+    HStep h;
+    if (is_zero(u01) && is_zero(u10)) {  // diagonal
+        const int c0 = unit_code(u00), c1 = unit_code(u11);
+        if (c0 == 0 && c1 == 0) return;  // identity
+        h.diagonal = true;
+        if (c0 == 0) {
+            h.s = blank_step(ST_PHASE);
+            h.s.cm = g.cm | (1ull << g.t);
+            set_entry(h.s, 0, u11);
+            h.unit = c1 >= 0;
+            h.s.unit = h.unit;
+            h.s.u0 = (uint8_t)(c1 < 0 ? 0 : c1);
+            h.dcm = h.s.cm;
+            h.d1 = u11;
+        } else {
+            h.s = blank_step(ST_DIAG);
+            h.s.cm = g.cm;
+            h.s.fb = (uint8_t)g.t;
+            set_entry(h.s, 0, u00);
+            set_entry(h.s, 1, u11);
+            h.unit = c0 >= 0 && c1 >= 0;
+            h.s.unit = h.unit;
+            h.s.u0 = (uint8_t)(c0 < 0 ? 0 : c0);
+            h.s.u1 = (uint8_t)(c1 < 0 ? 0 : c1);
+            h.dcm = g.cm;
+            h.dfb = g.t;
+            h.d0 = u00;
+            h.d1 = u11;
+        }
+        out.push_back(h);
+        return;
+    }
+    if (is_zero(u00) && is_zero(u11) && unit_code(u01) >= 0 && unit_code(u10) >= 0) {
+        h.s = blank_step(ST_PERM);
+        h.s.anti = 1;
+        h.s.u0 = (uint8_t)unit_code(u01);
+        h.s.u1 = (uint8_t)unit_code(u10);
+        h.s.unit = 1;
+        h.unit = true;
+    } else if (u00.imag() == 0 && u01.imag() == 0 && u10.imag() == 0 && u11.imag() == 0) {
+        h.s = blank_step(ST_REAL);
+    } else {
+        h.s = blank_step(ST_DENSE);
+    }
+    h.s.cm = g.cm;
+    set_entry(h.s, 0, u00);
+    set_entry(h.s, 1, u01);
+    set_entry(h.s, 2, u10);
+    set_entry(h.s, 3, u11);
+    h.need[0] = g.t;
+    out.push_back(h);
+}
+
+// Tries to fold a run of diagonal steps into one TABLE step. Returns false when the run's bits
+// do not fit MAX_TABLE_FIELDS fields of MAX_TABLE_BITS contiguous bits.
+bool fold_table(const std::vector<HStep>& run, Plan* plan, HStep* out) {
+    uint64_t common = ~0ull;
+    for (const HStep& h : run) common &= h.dcm;
+    // bits each step depends on beyond the common condition
+    std::vector<uint64_t> rest(run.size());
+    uint64_t uni = 0;
+    for (size_t i = 0; i < run.size(); ++i) {
+        uint64_t r = run[i].dcm & ~common;
+        if (run[i].dfb >= 0) r |= 1ull << run[i].dfb;
+        rest[i] = r;
+        uni |= r;
+    }
+    int lo[MAX_TABLE_FIELDS], width[MAX_TABLE_FIELDS], nf = 0;
+    uint64_t left = uni;
+    while (left) {
+        if (nf == MAX_TABLE_FIELDS) return false;
+        const int b = __builtin_ctzll(left);
+        lo[nf] = b;
+        int w = 0;
+        for (int q = b; q < 64 && q < b + MAX_TABLE_BITS; ++q)
+            if ((left >> q) & 1ull) w = q - b + 1;
+        width[nf] = w;
+        const uint64_t fm = (w >= 64) ? ~0ull : (((1ull << w) - 1ull) << b);
+        left &= ~fm;
+        ++nf;
+    }
+    if (nf == 0) {  // every step depends only on the common condition: one constant factor
+        lo[0] = 0;
+        width[0] = 0;
+        nf = 1;
+    }
+    std::vector<int> field(run.size(), 0);
+    for (size_t i = 0; i < run.size(); ++i) {
+        if (!rest[i]) continue;
+        int f = -1;
+        for (int q = 0; q < nf; ++q) {
+            const uint64_t fm = ((1ull << width[q]) - 1ull) << lo[q];
+            if ((rest[i] & ~fm) == 0) { f = q; break; }
+        }
+        if (f < 0) return false;
+        field[i] = f;
+    }
+    HStep h;
+    h.s = blank_step(ST_TABLE);
+    h.s.cm = common == ~0ull ? 0 : common;
+    h.s.nfields = (uint8_t)nf;
+    h.diagonal = true;
+    for (int q = 0; q < nf; ++q) {
+        const size_t entries = (size_t)1 << width[q];
+        h.s.tab_off[q] = (uint32_t)(plan->table_f64.size() / 2);
+        h.s.tab_shift[q] = (uint8_t)lo[q];
+        h.s.tab_width[q] = (uint8_t)width[q];
+        for (size_t y = 0; y < entries; ++y) {
+            const uint64_t idx = (uint64_t)y << lo[q];
+            std::complex<long double> acc(1.0L, 0.0L);
+            for (size_t i = 0; i < run.size(); ++i) {
+                if (field[i] != q) continue;
+                const HStep& s = run[i];
+                const uint64_t need = s.dcm & ~common;
+                if ((idx & need) != need) continue;
+                cd f = s.d1;
+                if (s.dfb >= 0) f = ((idx >> s.dfb) & 1ull) ? s.d1 : s.d0;
+                acc *= std::complex<long double>(f.real(), f.imag());
+            }
+            const cd v((double)acc.real(), (double)acc.imag());
+            plan->table_f64.push_back(v.real());
+            plan->table_f64.push_back(v.imag());
+            float ff[4];
+            put_ff(ff, v);
+            plan->table_ff.insert(plan->table_ff.end(), ff, ff + 4);
+        }
+    }
+    *out = h;
+    return true;
+}
+
+}  // namespace
+
+int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
+               const uint8_t* none, size_t n_none, const PlanOptions& opt, Plan* plan) {
+    plan->passes.clear();
+    plan->customs.clear();
+    plan->table_ff.clear();
+    plan->table_f64.clear();
+    const int max_bits = std::max(1, std::min(opt.max_bits, std::min(n, MAX_TILE_BITS)));
+
+    // 1. ops -> AGates (controlled-2x2 form where possible), merging single-wire runs.
+    std::vector<AGate> gates;
+    std::vector<int> pending(n, -1);  // per bit: index in `gates` of an open single-wire run
+    auto close_bits = [&](uint64_t mask) {
+        for (int b = 0; b < n; ++b)
+            if (((mask >> b) & 1ull) && pending[b] >= 0) pending[b] = -1;
+    };
+    for (size_t g = 0; g < n_ops; ++g) {
+        const qgpu_op& op = ops[g];
+        if (op.kind == QGPU_GATE_ID) continue;
+        LocalGate lg;
+        int st = tabulate(op, n, mats, n_mats, none, n_none, &lg);
+        if (st != QGPU_OK) return st;
+        const int k = lg.k;
+        const size_t d = (size_t)1 << k;
+        // Effective linear map of the gate (Custom None rule folded in, simulation.rs:120-133):
+        // E[l][j] = none[l] ? delta(l, j) : (none[j] ? 0 : M[l][j]).
+        std::vector<cd> E(d * d);
+        for (size_t j = 0; j < d; ++j)
+            for (size_t l = 0; l < d; ++l)
+                E[j * d + l] = lg.none[l] ? cd(l == j ? 1.0 : 0.0, 0.0)
+                                          : (lg.none[j] ? cd(0, 0) : lg.M[j * d + l]);
+        uint64_t support = 0;
+        int bitpos[QGPU_MAX_OP_WIRES];
+        for (int m = 0; m < k; ++m) {
+            bitpos[m] = n - 1 - lg.wires[m];
+            support |= 1ull << bitpos[m];
+        }
+        // controlled-2x2 form: every column whose control bits are not all 1 is the identity
+        bool controlled = op.kind != QGPU_GATE_SWAP;
+        const size_t call = (d - 1) & ~(size_t)1;  // local index with every control bit set
+        for (size_t j = 0; j < d && controlled; ++j)
+            for (size_t l = 0; l < d && controlled; ++l) {
+                const bool in_block = ((j & call) == call) && ((l & call) == call);
+                if (in_block) continue;
+                if (E[j * d + l] != cd(l == j ? 1.0 : 0.0, 0.0)) controlled = false;
+            }
+        if (op.kind == QGPU_GATE_SWAP) {
+            close_bits(support);
+            AGate a;
+            a.kind = AGate::SWAP;
+            a.a = bitpos[1];
+            a.b = bitpos[0];
+            a.support = support;
+            gates.push_back(a);
+            continue;
+        }
+        if (!controlled) {
+            close_bits(support);
+            AGate a;
+            a.kind = AGate::BLOCK;
+            a.block = (int)plan->customs.size();
+            a.support = support;
+            plan->customs.push_back(lg);
+            gates.push_back(a);
+            continue;
+        }
+        AGate a;
+        a.kind = AGate::ONE;
+        a.t = bitpos[k - 1];
+        a.cm = support & ~(1ull << a.t);
+        a.support = support;
+        for (int lo = 0; lo < 2; ++lo)
+            for (int in = 0; in < 2; ++in) a.u[lo][in] = E[(call | in) * d + (call | lo)];
+        if (k == 1 && opt.merge_1q && pending[a.t] >= 0) {
+            AGate& p = gates[pending[a.t]];  // new = a.u * p.u
+            cd r[2][2];
+            for (int lo = 0; lo < 2; ++lo)
+                for (int in = 0; in < 2; ++in)
+                    r[lo][in] = a.u[lo][0] * p.u[0][in] + a.u[lo][1] * p.u[1][in];
+            std::memcpy(p.u, r, sizeof(r));
+            continue;
+        }
+        close_bits(support);
+        gates.push_back(a);
+        if (k == 1 && opt.merge_1q) pending[a.t] = (int)gates.size() - 1;
+    }
+
+    // 2. AGates -> steps.
+    std::vector<HStep> steps;
+    std::vector<int> block_at;  // steps index -> custom block (or -1)
+    for (const AGate& g : gates) {
+        if (g.kind == AGate::BLOCK) {
+            HStep h;
+            h.s = blank_step(0xFF);
+            h.s.lb = 0;
+            steps.push_back(h);
+            block_at.resize(steps.size(), -1);
+            block_at.back() = g.block;
+            continue;
+        }
+        if (g.kind == AGate::SWAP) {
+            HStep h;
+            h.s = blank_step(ST_SWAP);
+            h.need[0] = g.a;
+            h.need[1] = g.b;
+            h.unit = true;
+            steps.push_back(h);
+            continue;
+        }
+        emit_one(g, steps);
+    }
+    block_at.resize(steps.size(), -1);
+
+    // 3. fold runs of diagonal steps into phase tables.
+    if (opt.fuse_diagonal) {
+        std::vector<HStep> folded;
+        std::vector<int> folded_block;
+        size_t i = 0;
+        while (i < steps.size()) {
+            if (!steps[i].diagonal || block_at[i] >= 0) {
+                folded.push_back(steps[i]);
+                folded_block.push_back(block_at[i]);
+                ++i;
+                continue;
+            }
+            size_t j = i;
+            int general = 0;
+            while (j < steps.size() && steps[j].diagonal && block_at[j] < 0) {
+                general += steps[j].unit ? 0 : 1;
+                ++j;
+            }
+            HStep t;
+            std::vector<HStep> run(steps.begin() + i, steps.begin() + j);
+            if (general >= 2 && fold_table(run, plan, &t)) {
+                folded.push_back(t);
+                folded_block.push_back(-1);
+            } else {
+                for (size_t q = i; q < j; ++q) {
+                    folded.push_back(steps[q]);
+                    folded_block.push_back(-1);
+                }
+            }
+            i = j;
+        }
+        steps.swap(folded);
+        block_at.swap(folded_block);
+    }
+
+    // 4. group steps into register-tile passes.
+    const int conv = opt.policy == POL_FF ? 40 : 0;
+    Pass cur;
+    std::vector<int> cur_bits;
+    std::vector<HStep> cur_steps;
+    int cur_cost = 0;
+    bool cur_arith = false;
+    auto flush = [&]() {
+        if (cur_steps.empty()) return;
+        Pass p;
+        std::sort(cur_bits.begin(), cur_bits.end());
+        if (cur_bits.empty()) cur_bits.push_back(0);
+        p.nbits = (int)cur_bits.size();
+        for (int m = 0; m < p.nbits; ++m) p.bits[m] = cur_bits[m];
+        auto local = [&](int b) -> uint8_t {
+            for (int m = 0; m < p.nbits; ++m)
+                if (cur_bits[m] == b) return (uint8_t)m;
+            return 0;
+        };
+        for (HStep& h : cur_steps) {
+            if (h.need[0] >= 0) h.s.lb = local(h.need[0]);
+            if (h.need[1] >= 0) h.s.lb2 = local(h.need[1]);
+            p.steps.push_back(h.s);
+        }
+        p.arith = cur_arith;
+        p.cost = cur_cost;
+        plan->passes.push_back(p);
+        cur_bits.clear();
+        cur_steps.clear();
+        cur_cost = 0;
+        cur_arith = false;
+    };
+    for (size_t i = 0; i < steps.size(); ++i) {
+        if (block_at[i] >= 0) {
+            flush();
+            Pass p;
+            p.custom = block_at[i];
+            plan->passes.push_back(p);
+            continue;
+        }
+        const HStep& h = steps[i];
+        std::vector<int> bits = cur_bits;
+        for (int q = 0; q < 2; ++q)
+            if (h.need[q] >= 0 && std::find(bits.begin(), bits.end(), h.need[q]) == bits.end())
+                bits.push_back(h.need[q]);
+        const int c = step_cost(h, opt.policy);
+        const bool arith = !h.unit;
+        const int new_cost = cur_cost + c + ((arith && !cur_arith) ? conv : 0);
+        const bool fits = (int)bits.size() <= max_bits && (int)cur_steps.size() < MAX_STEPS &&
+                          (cur_steps.empty() || new_cost <= opt.budget);
+        if (!fits) {
+            flush();
+            bits.clear();
+            for (int q = 0; q < 2; ++q)
+                if (h.need[q] >= 0 && std::find(bits.begin(), bits.end(), h.need[q]) == bits.end())
+                    bits.push_back(h.need[q]);
+        }
+        cur_bits = bits;
+        cur_cost += c + ((arith && !cur_arith) ? conv : 0);
+        cur_arith = cur_arith || arith;
+        cur_steps.push_back(h);
+    }
+    flush();
+    return QGPU_OK;
+}
+
+}  // namespace qgpu

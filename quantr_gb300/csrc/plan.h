@@ -1,0 +1,95 @@
+// plan.h — host-side gate tabulation and pass planning shared by the kernels' launchers.
+#pragma once
+
+#include <stdint.h>
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "../../include/qgpu.h"
+
+namespace qgpu {
+
+using cd = std::complex<double>;
+
+// ---------------------------------------------------------------------------------------------
+// One gate as the reference applies it: a local register of k wires [controls..., target]
+// (first = most significant local bit) and the 2^k images of its basis states.
+// ---------------------------------------------------------------------------------------------
+struct LocalGate {
+    int k = 1;
+    int wires[QGPU_MAX_OP_WIRES];  // acting positions, local bit order (MSB first)
+    std::vector<cd> M;             // column-major: M[j * 2^k + l] = image of input j at output l
+    std::vector<uint8_t> none;     // none[j] = 1 when the Custom function returned None for j
+};
+
+// Number of wires an op acts on; validates wires against n. Returns QGPU_OK or an error code
+// with the message set.
+int op_arity(const qgpu_op& op, int n, int* k_out);
+// Tabulates an op with the reference's gate formulas (standard_gate_ops.rs:37-267) or the
+// host-evaluated Custom table.
+int tabulate(const qgpu_op& op, int n, const double* mats, size_t n_mats, const uint8_t* none,
+             size_t n_none, LocalGate* out);
+
+// ---------------------------------------------------------------------------------------------
+// Fused passes for the fast kernels (QGPU_MODE_FAST / QGPU_MODE_F64 / complex64).
+// ---------------------------------------------------------------------------------------------
+enum StepType : uint8_t {
+    ST_DENSE = 0,  // 2x2 complex on tile bit lb
+    ST_REAL = 1,   // 2x2 real on tile bit lb
+    ST_PERM = 2,   // monomial 2x2 with entries in {1, i, -1, -i} on tile bit lb (anti = swap)
+    ST_SWAP = 3,   // exchange tile bits lb and lb2
+    ST_PHASE = 4,  // v *= d where (index & cm) == cm (any bits; unit d uses no arithmetic)
+    ST_DIAG = 5,   // v *= (index bit fb) ? d1 : d0, under (index & cm) == cm
+    ST_TABLE = 6,  // v *= prod_f T_f[(index >> shift_f) & (2^width_f - 1)], under cm
+};
+
+constexpr int MAX_TILE_BITS = 3;
+constexpr int MAX_STEPS = 24;
+constexpr int MAX_TABLE_FIELDS = 3;
+constexpr int MAX_TABLE_BITS = 11;
+
+// Step as seen by the device: FF constants (re_h, re_l, im_h, im_l per complex), f64 and f32
+// copies, so one table serves every arithmetic policy.
+struct DevStep {
+    uint8_t type, lb, lb2, fb;
+    uint8_t anti, u0, u1, unit;        // PERM: out0 = i^u0 * v[anti], out1 = i^u1 * v[!anti]
+    uint64_t cm;                       // control mask on the full index
+    uint32_t tab_off[MAX_TABLE_FIELDS];  // TABLE: entry offsets into the pass table buffer
+    uint8_t tab_shift[MAX_TABLE_FIELDS], tab_width[MAX_TABLE_FIELDS];
+    uint8_t nfields, pad[3];
+    float ff[16];                      // up to 4 complex entries as float pairs
+    double d[8];                       // the same entries in f64
+};
+
+struct Pass {
+    int nbits = 0;                     // tile bits
+    int bits[MAX_TILE_BITS];           // full-index bit positions, ascending
+    bool arith = false;                // needs float-pair / f64 arithmetic
+    int cost = 0;                      // planner's ops-per-amplitude estimate
+    std::vector<DevStep> steps;
+    int custom = -1;                   // >= 0: this pass is a Custom gate (group kernel)
+};
+
+struct Plan {
+    std::vector<Pass> passes;
+    std::vector<LocalGate> customs;    // Custom gates, run by the group kernel
+    std::vector<float> table_ff;       // TABLE entries as float pairs (4 floats each)
+    std::vector<double> table_f64;     // TABLE entries as f64 (2 doubles each)
+};
+
+enum ArithPolicy { POL_FF = 0, POL_F64 = 1, POL_F32 = 2 };
+
+struct PlanOptions {
+    int policy = POL_FF;               // arithmetic the passes will run in (sets step costs)
+    int max_bits = MAX_TILE_BITS;      // tile width (register tile of 2^bits amplitudes)
+    int budget = 100;                  // arithmetic ops per amplitude a pass may carry
+    bool merge_1q = true;              // multiply runs of single-wire gates into one matrix
+    bool fuse_diagonal = true;         // fold diagonal runs into phase tables
+};
+
+int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
+               const uint8_t* none, size_t n_none, const PlanOptions& opt, Plan* plan);
+
+}  // namespace qgpu

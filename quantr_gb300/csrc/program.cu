@@ -1,0 +1,703 @@
+// program.cu — qgpu_apply_program: the device side of `simulate_with_register`
+// (src/circuit/simulation.rs:21-57) and `apply_gate` (simulation.rs:64-135).
+//
+// Two execution paths:
+//  * QGPU_MODE_EXACT (complex128): one launch of k_group per gate. Each CTA stages whole
+//    gate groups (the 2^k amplitudes that share all non-acting bits) in shared memory and writes
+//    out[l] = none[l] ? a[l] : sum over non-None inputs j, in increasing full index, of
+//    M[l][j] * a[j] — f64 products and sums without contraction, first product assigned then
+//    added to (simulation.rs:168-179) — so amplitudes equal the reference's.
+//  * fused (QGPU_MODE_FAST / QGPU_MODE_F64 / complex64): the planner (plan.cpp) turns the gate
+//    list into register-tile passes. k_tile<K> gives each thread 2^K amplitudes that differ in
+//    the pass's K tile bits, applies every step of the pass in registers and writes them back:
+//    one HBM round trip per pass.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.cuh"
+#include "plan.h"
+
+namespace qgpu {
+
+// =============================================================================================
+// Exact group kernel
+// =============================================================================================
+struct GroupArgs {
+    uint64_t ngroups;
+    int k;
+    int nbits_sorted;
+    int sorted_bits[QGPU_MAX_OP_WIRES];   // acting bit positions, ascending (for base insertion)
+    const uint64_t* scatter;              // [2^k] offset of local index l
+    const int* order;                     // [2^k] local inputs in increasing full index
+    const double2* M;                     // [2^k * 2^k] column-major images
+    const uint8_t* none;                  // [2^k]
+    int groups_per_block;
+};
+
+template <class S>
+__device__ __forceinline__ double2 ld_amp(const S* s, uint64_t i) {
+    return make_double2((double)s[i].x, (double)s[i].y);
+}
+__device__ __forceinline__ void st_amp(double2* s, uint64_t i, double2 v) { s[i] = v; }
+__device__ __forceinline__ void st_amp(float2* s, uint64_t i, double2 v) {
+    s[i] = make_float2((float)v.x, (float)v.y);
+}
+
+template <class S>
+__global__ void __launch_bounds__(256) k_group(S* __restrict__ st, GroupArgs a) {
+    extern __shared__ double2 sh[];
+    const int dk = 1 << a.k;
+    const int per = a.groups_per_block * dk;
+    for (uint64_t g0 = (uint64_t)blockIdx.x * a.groups_per_block; g0 < a.ngroups;
+         g0 += (uint64_t)gridDim.x * a.groups_per_block) {
+        for (int t = threadIdx.x; t < per; t += blockDim.x) {
+            const uint64_t g = g0 + (t >> a.k);
+            if (g >= a.ngroups) continue;
+            uint64_t base = g;
+            for (int m = 0; m < a.nbits_sorted; ++m) base = insert_zero(base, a.sorted_bits[m]);
+            sh[t] = ld_amp(st, base | a.scatter[t & (dk - 1)]);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < per; t += blockDim.x) {
+            const uint64_t g = g0 + (t >> a.k);
+            if (g >= a.ngroups) continue;
+            const int l = t & (dk - 1);
+            const double2* grp = sh + (t >> a.k) * dk;
+            double2 out = grp[l];
+            if (!a.none[l]) {
+                bool first = true;
+                for (int q = 0; q < dk; ++q) {
+                    const int j = a.order[q];
+                    if (a.none[j]) continue;
+                    const double2 m = a.M[(size_t)j * dk + l];
+                    const double2 x = grp[j];
+                    // num-complex Mul (image * amplitude), no FMA contraction
+                    const double pr = __dsub_rn(__dmul_rn(m.x, x.x), __dmul_rn(m.y, x.y));
+                    const double pi = __dadd_rn(__dmul_rn(m.x, x.y), __dmul_rn(m.y, x.x));
+                    if (first) {
+                        out = make_double2(pr, pi);
+                        first = false;
+                    } else {
+                        out = make_double2(__dadd_rn(out.x, pr), __dadd_rn(out.y, pi));
+                    }
+                }
+            }
+            uint64_t base = g;
+            for (int m = 0; m < a.nbits_sorted; ++m) base = insert_zero(base, a.sorted_bits[m]);
+            st_amp(st, base | a.scatter[l], out);
+        }
+        __syncthreads();
+    }
+}
+
+// Device copy of one gate's tables, laid out in the handle's gate scratch.
+struct GroupTables {
+    size_t scatter_off, order_off, m_off, none_off, bytes;
+};
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+static GroupTables group_layout(int k, size_t at) {
+    const size_t d = (size_t)1 << k;
+    GroupTables t;
+    t.scatter_off = align_up(at, 256);
+    t.order_off = align_up(t.scatter_off + d * 8, 16);
+    t.m_off = align_up(t.order_off + d * 4, 16);
+    t.none_off = align_up(t.m_off + d * d * 16, 16);
+    t.bytes = align_up(t.none_off + d, 256) - at;
+    return t;
+}
+
+static void group_fill(const LocalGate& g, int n, std::vector<uint8_t>& host, size_t at,
+                       const GroupTables& t, GroupArgs* args) {
+    const int k = g.k;
+    const size_t d = (size_t)1 << k;
+    uint64_t* scatter = (uint64_t*)(host.data() + t.scatter_off);
+    int* order = (int*)(host.data() + t.order_off);
+    double2* M = (double2*)(host.data() + t.m_off);
+    uint8_t* none = host.data() + t.none_off;
+    for (size_t l = 0; l < d; ++l) {
+        uint64_t off = 0;
+        for (int m = 0; m < k; ++m)
+            if ((l >> (k - 1 - m)) & 1u) off |= 1ull << (n - 1 - g.wires[m]);
+        scatter[l] = off;
+        order[l] = (int)l;
+        none[l] = g.none[l];
+    }
+    std::sort(order, order + d, [&](int x, int y) { return scatter[x] < scatter[y]; });
+    for (size_t j = 0; j < d; ++j)
+        for (size_t l = 0; l < d; ++l)
+            M[j * d + l] = make_double2(g.M[j * d + l].real(), g.M[j * d + l].imag());
+    args->k = k;
+    args->nbits_sorted = k;
+    int sb[QGPU_MAX_OP_WIRES];
+    for (int m = 0; m < k; ++m) sb[m] = n - 1 - g.wires[m];
+    std::sort(sb, sb + k);
+    for (int m = 0; m < k; ++m) args->sorted_bits[m] = sb[m];
+    (void)at;
+}
+
+static int launch_group(qgpu_handle* h, const GroupArgs& a0, const uint8_t* dev_base,
+                        const GroupTables& t) {
+    GroupArgs a = a0;
+    a.scatter = (const uint64_t*)(dev_base + t.scatter_off);
+    a.order = (const int*)(dev_base + t.order_off);
+    a.M = (const double2*)(dev_base + t.m_off);
+    a.none = dev_base + t.none_off;
+    const int dk = 1 << a.k;
+    a.groups_per_block = dk >= 256 ? 1 : 256 / dk;
+    a.ngroups = h->dim >> a.k;
+    if ((uint64_t)a.groups_per_block > a.ngroups) a.groups_per_block = (int)a.ngroups;
+    const size_t smem = (size_t)a.groups_per_block * dk * sizeof(double2);
+    uint64_t blocks = (a.ngroups + a.groups_per_block - 1) / a.groups_per_block;
+    const uint64_t cap = (uint64_t)h->sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    if (smem > 48 * 1024) {
+        cudaError_t e = (h->precision == QGPU_C128)
+                            ? cudaFuncSetAttribute(k_group<double2>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                            : cudaFuncSetAttribute(k_group<float2>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_group)");
+    }
+    if (h->precision == QGPU_C128)
+        k_group<double2><<<(unsigned)blocks, 256, smem, h->stream>>>((double2*)h->state, a);
+    else
+        k_group<float2><<<(unsigned)blocks, 256, smem, h->stream>>>((float2*)h->state, a);
+    QGPU_CHECK_LAUNCH("k_group");
+    h->launches++;
+    return QGPU_OK;
+}
+
+// Uploads the tables of `gates` and runs one k_group launch per gate.
+static int run_groups(qgpu_handle* h, const std::vector<const LocalGate*>& gates) {
+    if (gates.empty()) return QGPU_OK;
+    std::vector<GroupTables> lay(gates.size());
+    size_t at = 0;
+    for (size_t i = 0; i < gates.size(); ++i) {
+        lay[i] = group_layout(gates[i]->k, at);
+        at = align_up(lay[i].none_off + ((size_t)1 << gates[i]->k), 256);
+    }
+    std::vector<uint8_t> host(at, 0);
+    std::vector<GroupArgs> args(gates.size());
+    for (size_t i = 0; i < gates.size(); ++i) {
+        std::memset(&args[i], 0, sizeof(GroupArgs));
+        group_fill(*gates[i], h->n_qubits, host, 0, lay[i], &args[i]);
+    }
+    int st = h->gates.ensure(at);
+    if (st != QGPU_OK) return st;
+    QGPU_CUDA(cudaMemcpyAsync(h->gates.ptr, host.data(), at, cudaMemcpyHostToDevice, h->stream));
+    for (size_t i = 0; i < gates.size(); ++i) {
+        st = launch_group(h, args[i], (const uint8_t*)h->gates.ptr, lay[i]);
+        if (st != QGPU_OK) return st;
+    }
+    // the host staging buffer must outlive the async copy
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    return QGPU_OK;
+}
+
+// =============================================================================================
+// Register-tile kernels
+// =============================================================================================
+struct TileParams {
+    uint64_t ngroups;
+    const float4* tab_ff;     // TABLE entries, float pairs
+    const double2* tab_f64;   // TABLE entries, f64
+    int nbits;
+    int bits[MAX_TILE_BITS];
+    int nsteps;
+    DevStep steps[MAX_STEPS];
+};
+
+// multiply by i^code on any complex representation
+template <class R>
+__device__ __forceinline__ void unit_mul(R& a, int code);
+
+template <>
+__device__ __forceinline__ void unit_mul<ffc>(ffc& a, int code) {
+    if (code == 1) {
+        ffc r{-a.ih, -a.il, a.rh, a.rl};
+        a = r;
+    } else if (code == 2) {
+        ffc r{-a.rh, -a.rl, -a.ih, -a.il};
+        a = r;
+    } else if (code == 3) {
+        ffc r{a.ih, a.il, -a.rh, -a.rl};
+        a = r;
+    }
+}
+template <>
+__device__ __forceinline__ void unit_mul<double2>(double2& a, int code) {
+    if (code == 1) a = make_double2(-a.y, a.x);
+    else if (code == 2) a = make_double2(-a.x, -a.y);
+    else if (code == 3) a = make_double2(a.y, -a.x);
+}
+template <>
+__device__ __forceinline__ void unit_mul<float2>(float2& a, int code) {
+    if (code == 1) a = make_float2(-a.y, a.x);
+    else if (code == 2) a = make_float2(-a.x, -a.y);
+    else if (code == 3) a = make_float2(a.y, -a.x);
+}
+
+// ---- float-pair policy: complex128 storage, f64 arithmetic emulated on FP32/INT pipes -------
+struct PolFF {
+    using S = double2;
+    using R = ffc;
+    static __device__ __forceinline__ R load(S a) { return to_ffc(a); }
+    static __device__ __forceinline__ S store(const R& r) { return from_ffc(r); }
+    // out0 = u00 a + u01 b ; out1 = u10 a + u11 b ; m = 4 float-pair complex entries
+    static __device__ __forceinline__ void dense(R& a, R& b, const float* m) {
+        Dot2 d;
+        R o0, o1;
+        d.first(m[0], m[1], a.rh, a.rl);
+        d.add(-m[2], -m[3], a.ih, a.il);
+        d.add(m[4], m[5], b.rh, b.rl);
+        d.add(-m[6], -m[7], b.ih, b.il);
+        d.result(o0.rh, o0.rl);
+        d.first(m[0], m[1], a.ih, a.il);
+        d.add(m[2], m[3], a.rh, a.rl);
+        d.add(m[4], m[5], b.ih, b.il);
+        d.add(m[6], m[7], b.rh, b.rl);
+        d.result(o0.ih, o0.il);
+        d.first(m[8], m[9], a.rh, a.rl);
+        d.add(-m[10], -m[11], a.ih, a.il);
+        d.add(m[12], m[13], b.rh, b.rl);
+        d.add(-m[14], -m[15], b.ih, b.il);
+        d.result(o1.rh, o1.rl);
+        d.first(m[8], m[9], a.ih, a.il);
+        d.add(m[10], m[11], a.rh, a.rl);
+        d.add(m[12], m[13], b.ih, b.il);
+        d.add(m[14], m[15], b.rh, b.rl);
+        d.result(o1.ih, o1.il);
+        a = o0;
+        b = o1;
+    }
+    static __device__ __forceinline__ void real(R& a, R& b, const float* m) {
+        Dot2 d;
+        R o0, o1;
+        d.first(m[0], m[1], a.rh, a.rl);
+        d.add(m[4], m[5], b.rh, b.rl);
+        d.result(o0.rh, o0.rl);
+        d.first(m[0], m[1], a.ih, a.il);
+        d.add(m[4], m[5], b.ih, b.il);
+        d.result(o0.ih, o0.il);
+        d.first(m[8], m[9], a.rh, a.rl);
+        d.add(m[12], m[13], b.rh, b.rl);
+        d.result(o1.rh, o1.rl);
+        d.first(m[8], m[9], a.ih, a.il);
+        d.add(m[12], m[13], b.ih, b.il);
+        d.result(o1.ih, o1.il);
+        a = o0;
+        b = o1;
+    }
+    static __device__ __forceinline__ void mul(R& a, float ch, float cl, float sh_, float sl) {
+        Dot2 d;
+        R o;
+        d.first(ch, cl, a.rh, a.rl);
+        d.add(-sh_, -sl, a.ih, a.il);
+        d.result(o.rh, o.rl);
+        d.first(ch, cl, a.ih, a.il);
+        d.add(sh_, sl, a.rh, a.rl);
+        d.result(o.ih, o.il);
+        a = o;
+    }
+    static __device__ __forceinline__ void mul_slot(R& a, const DevStep& s, int slot) {
+        mul(a, s.ff[4 * slot], s.ff[4 * slot + 1], s.ff[4 * slot + 2], s.ff[4 * slot + 3]);
+    }
+    static __device__ __forceinline__ void mul_table(R& a, const TileParams& p, uint32_t e) {
+        const float4 c = __ldg(p.tab_ff + e);
+        mul(a, c.x, c.y, c.z, c.w);
+    }
+};
+
+// ---- native f64 policy (FMA), for comparison ----------------------------------------------
+struct PolF64 {
+    using S = double2;
+    using R = double2;
+    static __device__ __forceinline__ R load(S a) { return a; }
+    static __device__ __forceinline__ S store(const R& r) { return r; }
+    static __device__ __forceinline__ double2 cmla(double2 acc, double ur, double ui, double2 x) {
+        return make_double2(fma(ur, x.x, fma(-ui, x.y, acc.x)), fma(ur, x.y, fma(ui, x.x, acc.y)));
+    }
+    static __device__ __forceinline__ void dense(R& a, R& b, const double* m) {
+        double2 o0 = cmla(cmla(make_double2(0, 0), m[0], m[1], a), m[2], m[3], b);
+        double2 o1 = cmla(cmla(make_double2(0, 0), m[4], m[5], a), m[6], m[7], b);
+        a = o0;
+        b = o1;
+    }
+    static __device__ __forceinline__ void real(R& a, R& b, const double* m) {
+        double2 o0 = make_double2(fma(m[0], a.x, m[2] * b.x), fma(m[0], a.y, m[2] * b.y));
+        double2 o1 = make_double2(fma(m[4], a.x, m[6] * b.x), fma(m[4], a.y, m[6] * b.y));
+        a = o0;
+        b = o1;
+    }
+    static __device__ __forceinline__ void mul(R& a, double cr, double ci) {
+        a = make_double2(fma(cr, a.x, -ci * a.y), fma(cr, a.y, ci * a.x));
+    }
+    static __device__ __forceinline__ void mul_slot(R& a, const DevStep& s, int slot) {
+        mul(a, s.d[2 * slot], s.d[2 * slot + 1]);
+    }
+    static __device__ __forceinline__ void mul_table(R& a, const TileParams& p, uint32_t e) {
+        const double2 c = __ldg(p.tab_f64 + e);
+        mul(a, c.x, c.y);
+    }
+};
+
+// ---- complex64 policy ------------------------------------------------------------------------
+struct PolF32 {
+    using S = float2;
+    using R = float2;
+    static __device__ __forceinline__ R load(S a) { return a; }
+    static __device__ __forceinline__ S store(const R& r) { return r; }
+    static __device__ __forceinline__ float2 cmla(float2 acc, float ur, float ui, float2 x) {
+        return make_float2(fmaf(ur, x.x, fmaf(-ui, x.y, acc.x)), fmaf(ur, x.y, fmaf(ui, x.x, acc.y)));
+    }
+    static __device__ __forceinline__ void dense(R& a, R& b, const float* m) {
+        // hi parts of the float-pair entries are the entries rounded to f32
+        float2 o0 = cmla(cmla(make_float2(0, 0), m[0], m[2], a), m[4], m[6], b);
+        float2 o1 = cmla(cmla(make_float2(0, 0), m[8], m[10], a), m[12], m[14], b);
+        a = o0;
+        b = o1;
+    }
+    static __device__ __forceinline__ void real(R& a, R& b, const float* m) {
+        float2 o0 = make_float2(fmaf(m[0], a.x, m[4] * b.x), fmaf(m[0], a.y, m[4] * b.y));
+        float2 o1 = make_float2(fmaf(m[8], a.x, m[12] * b.x), fmaf(m[8], a.y, m[12] * b.y));
+        a = o0;
+        b = o1;
+    }
+    static __device__ __forceinline__ void mul(R& a, float cr, float ci) {
+        a = make_float2(fmaf(cr, a.x, -ci * a.y), fmaf(cr, a.y, ci * a.x));
+    }
+    static __device__ __forceinline__ void mul_slot(R& a, const DevStep& s, int slot) {
+        mul(a, s.ff[4 * slot], s.ff[4 * slot + 2]);
+    }
+    static __device__ __forceinline__ void mul_table(R& a, const TileParams& p, uint32_t e) {
+        const float4 c = __ldg(p.tab_ff + e);
+        mul(a, c.x, c.z);
+    }
+};
+
+// ---- data-movement-only policy (passes of permutations and +-1/+-i phases) -------------------
+template <class T>
+struct PolRaw {
+    using S = T;
+    using R = T;
+    static __device__ __forceinline__ R load(S a) { return a; }
+    static __device__ __forceinline__ S store(const R& r) { return r; }
+};
+
+template <class P>
+struct Consts;
+template <>
+struct Consts<PolFF> {
+    static __device__ __forceinline__ const float* m(const DevStep& s) { return s.ff; }
+};
+template <>
+struct Consts<PolF32> {
+    static __device__ __forceinline__ const float* m(const DevStep& s) { return s.ff; }
+};
+template <>
+struct Consts<PolF64> {
+    static __device__ __forceinline__ const double* m(const DevStep& s) { return s.d; }
+};
+
+template <class P>
+struct IsArith { static constexpr bool value = true; };
+template <class T>
+struct IsArith<PolRaw<T>> { static constexpr bool value = false; };
+
+// Applies step s to the 2^K amplitudes v of one tile (full indices base | off[j]).
+template <int K, int B, class P>
+__device__ __forceinline__ void step_on_bit(typename P::R* v, const DevStep& s, uint64_t base,
+                                            const uint64_t* off) {
+    constexpr int T = 1 << K;
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        if ((j >> B) & 1) continue;
+        const int j1 = j | (1 << B);
+        if (((base | off[j]) & s.cm) != s.cm) continue;
+        if (s.type == ST_PERM) {
+            typename P::R a = v[j], b = v[j1];
+            if (s.anti) {
+                v[j] = b;
+                v[j1] = a;
+            }
+            unit_mul(v[j], s.u0);
+            unit_mul(v[j1], s.u1);
+        } else {
+            if constexpr (IsArith<P>::value) {
+                if (s.type == ST_DENSE) P::dense(v[j], v[j1], Consts<P>::m(s));
+                else P::real(v[j], v[j1], Consts<P>::m(s));
+            }
+        }
+    }
+}
+
+// Exchange the amplitudes whose tile bits (A, B) read (0, 1) and (1, 0): the Swap gate.
+template <int K, int A, int B, class P>
+__device__ __forceinline__ void swap_bits(typename P::R* v) {
+#pragma unroll
+    for (int j = 0; j < (1 << K); ++j) {
+        if (((j >> A) & 1) == 0 && ((j >> B) & 1) == 1) {
+            const int j2 = (j | (1 << A)) & ~(1 << B);
+            typename P::R t = v[j];
+            v[j] = v[j2];
+            v[j2] = t;
+        }
+    }
+}
+
+template <int K, class P>
+__device__ __forceinline__ void step_tile(typename P::R* v, const DevStep& s, uint64_t base,
+                                          const uint64_t* off, const TileParams& p) {
+    constexpr int T = 1 << K;
+    switch (s.type) {
+        case ST_DENSE:
+        case ST_REAL:
+        case ST_PERM:
+            if (s.lb == 0) step_on_bit<K, 0, P>(v, s, base, off);
+            if constexpr (K > 1) if (s.lb == 1) step_on_bit<K, (K > 1 ? 1 : 0), P>(v, s, base, off);
+            if constexpr (K > 2) if (s.lb == 2) step_on_bit<K, (K > 2 ? 2 : 0), P>(v, s, base, off);
+            break;
+        case ST_SWAP: {
+            const int lo = s.lb < s.lb2 ? s.lb : s.lb2, hi = s.lb < s.lb2 ? s.lb2 : s.lb;
+            if constexpr (K >= 2) {
+                if (lo == 0 && hi == 1) swap_bits<K, 0, 1, P>(v);
+            }
+            if constexpr (K >= 3) {
+                if (lo == 0 && hi == 2) swap_bits<K, 0, (K >= 3 ? 2 : 1), P>(v);
+                if (lo == 1 && hi == 2) swap_bits<K, 1, (K >= 3 ? 2 : 1), P>(v);
+            }
+            break;
+        }
+        case ST_PHASE:
+#pragma unroll
+            for (int j = 0; j < T; ++j) {
+                if (((base | off[j]) & s.cm) != s.cm) continue;
+                if (s.unit) unit_mul(v[j], s.u0);
+                else if constexpr (IsArith<P>::value) P::mul_slot(v[j], s, 0);
+            }
+            break;
+        case ST_DIAG:
+#pragma unroll
+            for (int j = 0; j < T; ++j) {
+                const uint64_t idx = base | off[j];
+                if ((idx & s.cm) != s.cm) continue;
+                const int bit = (int)((idx >> s.fb) & 1ull);
+                if (s.unit) unit_mul(v[j], bit ? s.u1 : s.u0);
+                else if constexpr (IsArith<P>::value) P::mul_slot(v[j], s, bit);
+            }
+            break;
+        case ST_TABLE:
+            if constexpr (IsArith<P>::value) {
+#pragma unroll
+                for (int j = 0; j < T; ++j) {
+                    const uint64_t idx = base | off[j];
+                    if ((idx & s.cm) != s.cm) continue;
+                    for (int f = 0; f < s.nfields; ++f) {
+                        const uint32_t y =
+                            (uint32_t)((idx >> s.tab_shift[f]) & ((1ull << s.tab_width[f]) - 1ull));
+                        P::mul_table(v[j], p, s.tab_off[f] + y);
+                    }
+                }
+            }
+            break;
+        default:
+            break;
+    }
+}
+
+template <int K, int U, class P>
+__global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, const __grid_constant__ TileParams p) {
+    constexpr int T = 1 << K;
+    uint64_t off[T];
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        uint64_t o = 0;
+#pragma unroll
+        for (int m = 0; m < K; ++m)
+            if ((j >> m) & 1) o |= 1ull << p.bits[m];
+        off[j] = o;
+    }
+    const uint64_t chunk = (uint64_t)blockDim.x * U;
+    for (uint64_t g0 = (uint64_t)blockIdx.x * chunk; g0 < p.ngroups; g0 += (uint64_t)gridDim.x * chunk) {
+        uint64_t base[U];
+        typename P::S raw[U][T];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t g = g0 + (uint64_t)u * blockDim.x + threadIdx.x;
+            uint64_t b = g;
+#pragma unroll
+            for (int m = 0; m < K; ++m) b = insert_zero(b, p.bits[m]);
+            base[u] = b;
+            if (g < p.ngroups) {
+#pragma unroll
+                for (int j = 0; j < T; ++j) raw[u][j] = st[b | off[j]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t g = g0 + (uint64_t)u * blockDim.x + threadIdx.x;
+            if (g >= p.ngroups) continue;
+            typename P::R v[T];
+#pragma unroll
+            for (int j = 0; j < T; ++j) v[j] = P::load(raw[u][j]);
+            for (int s = 0; s < p.nsteps; ++s) step_tile<K, P>(v, p.steps[s], base[u], off, p);
+#pragma unroll
+            for (int j = 0; j < T; ++j) st[base[u] | off[j]] = P::store(v[j]);
+        }
+    }
+}
+
+template <int K, int U, class P>
+static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
+    const uint64_t per_block = 256ull * U;
+    uint64_t blocks = (p.ngroups + per_block - 1) / per_block;
+    const uint64_t cap = (uint64_t)h->sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_tile<K, U, P><<<(unsigned)blocks, 256, 0, h->stream>>>((typename P::S*)h->state, p);
+    QGPU_CHECK_LAUNCH("k_tile");
+    h->launches++;
+    return QGPU_OK;
+}
+
+template <class P>
+static int launch_tile_k(qgpu_handle* h, const TileParams& p) {
+    switch (p.nbits) {
+        case 1: return launch_tile_t<1, 4, P>(h, p);
+        case 2: return launch_tile_t<2, 2, P>(h, p);
+        default: return launch_tile_t<3, 1, P>(h, p);
+    }
+}
+
+static int policy_of(const qgpu_handle* h) {
+    if (h->precision == QGPU_C64) return POL_F32;
+    return h->mode == QGPU_MODE_F64 ? POL_F64 : POL_FF;
+}
+
+static int env_int(const char* name, int dflt) {
+    const char* v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    return std::atoi(v);
+}
+
+static int run_plan(qgpu_handle* h, const Plan& plan) {
+    const int pol = policy_of(h);
+    // phase tables for every TABLE step of the plan, uploaded once
+    const size_t nent = plan.table_f64.size() / 2;
+    const float4* tab_ff = nullptr;
+    const double2* tab_f64 = nullptr;
+    if (nent) {
+        const size_t ffb = align_up(nent * 16, 256);
+        int st = h->work2.ensure(ffb + nent * 16);
+        if (st != QGPU_OK) return st;
+        QGPU_CUDA(cudaMemcpyAsync(h->work2.ptr, plan.table_ff.data(), nent * 16,
+                                  cudaMemcpyHostToDevice, h->stream));
+        QGPU_CUDA(cudaMemcpyAsync((uint8_t*)h->work2.ptr + ffb, plan.table_f64.data(), nent * 16,
+                                  cudaMemcpyHostToDevice, h->stream));
+        tab_ff = (const float4*)h->work2.ptr;
+        tab_f64 = (const double2*)((uint8_t*)h->work2.ptr + ffb);
+    }
+    // Custom blocks: upload their tables once
+    std::vector<const LocalGate*> blocks;
+    for (const LocalGate& g : plan.customs) blocks.push_back(&g);
+    std::vector<GroupTables> lay(blocks.size());
+    std::vector<GroupArgs> gargs(blocks.size());
+    if (!blocks.empty()) {
+        size_t at = 0;
+        for (size_t i = 0; i < blocks.size(); ++i) {
+            lay[i] = group_layout(blocks[i]->k, at);
+            at = align_up(lay[i].none_off + ((size_t)1 << blocks[i]->k), 256);
+        }
+        std::vector<uint8_t> host(at, 0);
+        for (size_t i = 0; i < blocks.size(); ++i) {
+            std::memset(&gargs[i], 0, sizeof(GroupArgs));
+            group_fill(*blocks[i], h->n_qubits, host, 0, lay[i], &gargs[i]);
+        }
+        int st = h->gates.ensure(at);
+        if (st != QGPU_OK) return st;
+        QGPU_CUDA(cudaMemcpyAsync(h->gates.ptr, host.data(), at, cudaMemcpyHostToDevice, h->stream));
+        QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    TileParams tp;
+    for (const Pass& ps : plan.passes) {
+        if (ps.custom >= 0) {
+            int st = launch_group(h, gargs[ps.custom], (const uint8_t*)h->gates.ptr, lay[ps.custom]);
+            if (st != QGPU_OK) return st;
+            continue;
+        }
+        std::memset(&tp, 0, sizeof(tp));
+        tp.nbits = ps.nbits;
+        for (int m = 0; m < ps.nbits; ++m) tp.bits[m] = ps.bits[m];
+        tp.ngroups = h->dim >> ps.nbits;
+        tp.nsteps = (int)ps.steps.size();
+        for (int s = 0; s < tp.nsteps; ++s) tp.steps[s] = ps.steps[s];
+        tp.tab_ff = tab_ff;
+        tp.tab_f64 = tab_f64;
+        int st;
+        if (!ps.arith) {
+            st = (h->precision == QGPU_C64) ? launch_tile_k<PolRaw<float2>>(h, tp)
+                                            : launch_tile_k<PolRaw<double2>>(h, tp);
+        } else if (pol == POL_F32) {
+            st = launch_tile_k<PolF32>(h, tp);
+        } else if (pol == POL_F64) {
+            st = launch_tile_k<PolF64>(h, tp);
+        } else {
+            st = launch_tile_k<PolFF>(h, tp);
+        }
+        if (st != QGPU_OK) return st;
+    }
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    return QGPU_OK;
+}
+
+PlanOptions plan_options_for(const qgpu_handle* h) {
+    PlanOptions o;
+    o.policy = policy_of(h);
+    if (o.policy == POL_FF) o.budget = env_int("QGPU_FF_BUDGET", 140);
+    else if (o.policy == POL_F32) o.budget = env_int("QGPU_F32_BUDGET", 48);
+    else o.budget = env_int("QGPU_F64_BUDGET", 1 << 20);
+    o.max_bits = std::max(2, std::min(env_int("QGPU_TILE_BITS", MAX_TILE_BITS), MAX_TILE_BITS));
+    return o;
+}
+
+}  // namespace qgpu
+
+using namespace qgpu;
+
+extern "C" int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
+                                  const double* mats, size_t n_mat_doubles,
+                                  const uint8_t* none_flags, size_t n_none_flags) {
+    if (!h) return fail(QGPU_ERR_INVALID, "qgpu_apply_program: NULL handle");
+    if (n_ops && !ops) return fail(QGPU_ERR_INVALID, "qgpu_apply_program: ops is NULL");
+    if (n_ops == 0) return QGPU_OK;
+    if (h->precision == QGPU_C128 && h->mode == QGPU_MODE_EXACT) {
+        std::vector<LocalGate> gates;
+        gates.reserve(n_ops);
+        for (size_t g = 0; g < n_ops; ++g) {
+            if (ops[g].kind == QGPU_GATE_ID) continue;  // simulation.rs:38-41
+            LocalGate lg;
+            int st = tabulate(ops[g], h->n_qubits, mats, n_mat_doubles, none_flags, n_none_flags, &lg);
+            if (st != QGPU_OK) return st;
+            gates.push_back(std::move(lg));
+        }
+        // tables for a window of gates at a time keeps the device staging bounded
+        const size_t window = 512;
+        for (size_t i = 0; i < gates.size(); i += window) {
+            std::vector<const LocalGate*> part;
+            for (size_t j = i; j < gates.size() && j < i + window; ++j) part.push_back(&gates[j]);
+            int st = run_groups(h, part);
+            if (st != QGPU_OK) return st;
+        }
+        return QGPU_OK;
+    }
+    Plan plan;
+    int st = build_plan(ops, n_ops, h->n_qubits, mats, n_mat_doubles, none_flags, n_none_flags,
+                        plan_options_for(h), &plan);
+    if (st != QGPU_OK) return st;
+    return run_plan(h, plan);
+}

@@ -1,0 +1,149 @@
+"""Host-side logic of the quantr API mirror and the C-ABI library (no GPU needed).
+
+Mirrors the reference's builder/layout tests and its #[should_panic] error tests
+(src/circuit.rs:516-597, 715-720, 839-845, 984-991; product_states.rs:274-321).
+"""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from golden import quantr_goldens as G
+from quantr_gb300 import Circuit, Gate, ProductState, QuantrError, Qubit, SuperPosition
+from quantr_gb300 import _native
+from quantr_gb300 import workloads as W
+from quantr_gb300.program import OP_DTYPE, lower, tabulate_custom
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_pushes_multi_gates():  # src/circuit.rs:535-550
+    qc = Circuit(3)
+    qc.add_gates([Gate.CNot(2), Gate.CNot(0), Gate.H]).add_gates([Gate.Toffoli(1, 2), Gate.H,
+                                                                  Gate.CNot(0)])
+    assert qc.get_gates() == G.PUSHED_LAYOUT
+
+
+def test_pushes_multi_gates_using_vec():  # src/circuit.rs:553-575
+    qc = Circuit(3)
+    qc.add_gates_with_positions({2: Gate.H, 0: Gate.CNot(2), 1: Gate.CNot(0)}) \
+        .add_gates_with_positions({2: Gate.CNot(0), 0: Gate.Toffoli(1, 2), 1: Gate.H})
+    assert qc.get_gates() == G.PUSHED_LAYOUT
+
+
+def test_get_gates_pads_with_identity():  # circuit.rs:94-105
+    qc = Circuit(3)
+    qc.add_gate(Gate.X, 2)
+    assert qc.get_gates() == [Gate.Id, Gate.Id, Gate.X]
+
+
+@pytest.mark.parametrize("make", [
+    lambda: Circuit(3).add_gates([Gate.Id, Gate.Custom(G.example_cnot, [1], "X"), Gate.Id]),
+    lambda: Circuit(3).add_gates([Gate.CNot(0), Gate.Id, Gate.Id]),
+    lambda: Circuit(3).add_gates_with_positions({2: Gate.H, 0: Gate.CNot(0), 1: Gate.CNot(0)}),
+    lambda: Circuit(3).add_gates_with_positions({2: Gate.H, 0: Gate.CNot(2), 1: Gate.CNot(3)}),
+    lambda: Circuit(4).add_repeating_gate(Gate.X, [0, 1, 1, 3]),
+    lambda: Circuit(3).add_gate(Gate.Custom(G.example_cnot, [0], "NonAscii†"), 1),
+    lambda: Circuit(3).add_gate(Gate.X, 1).change_register(
+        SuperPosition.from_(ProductState([Qubit.One, Qubit.Zero]))),
+    lambda: Circuit(0),
+    lambda: Circuit(2).add_gates([Gate.H]),
+    lambda: Circuit(2).add_gate(Gate.H, 2),
+], ids=["overlapping_custom", "overlapping_control", "overlapping_vec", "control_too_big",
+        "repeating_positions", "non_ascii_name", "register_dimension", "zero_wires",
+        "column_length", "position_out_of_bounds"])
+def test_reference_error_cases_raise(make):
+    with pytest.raises(QuantrError):
+        make()
+
+
+def test_product_state_ordering():  # product_states.rs:274-321
+    assert ProductState.binary_basis(6, 3) == ProductState([Qubit.One, Qubit.One, Qubit.Zero])
+    assert ProductState([1, 0, 1]).comp_basis() == 5
+    assert ProductState([1, 1, 1]).comp_basis() == 7
+    assert ProductState([1, 0]).comp_basis() == 2
+    assert ProductState([1, 0, 1, 1]).comp_basis() == 11
+    p = ProductState([1, 1, 1])
+    p.insert_qubits([Qubit.Zero, Qubit.Zero], [0, 2])
+    assert p == ProductState([0, 1, 0])
+    assert str(ProductState([0, 1])) == "01"
+
+
+def test_superposition_constructors_and_checks():  # super_positions.rs:403-544
+    s = SuperPosition.new(2)
+    s.set_amplitudes([0, 2 ** -0.5, -1j * 2 ** -0.5, 0])
+    assert s.get_amplitude_from_state(ProductState([Qubit.Zero, Qubit.One])) == pytest.approx(2 ** -0.5)
+    assert s.get_amplitude(4) is None
+    with pytest.raises(QuantrError):
+        s.set_amplitudes([0, 0.5, 0, -0.5j])
+    with pytest.raises(QuantrError):
+        s.get_amplitude_from_state(ProductState([0, 1, 1]))
+    with pytest.raises(QuantrError):
+        SuperPosition.new_with_hash_amplitudes({ProductState([0, 1]): 2 ** -0.5,
+                                                ProductState([1, 0, 1]): -1j * 2 ** -0.5})
+    hm = SuperPosition.new_with_amplitudes([0, 2 ** -0.5, 2 ** -0.5, 0]).to_hash_map()
+    assert set(map(str, hm)) == {"01", "10"}
+    it = list(SuperPosition.new_with_amplitudes([0, 2 ** -0.5, 2 ** -0.5, 0]))
+    assert str(it[1][0]) == "01" and it[1][1] == pytest.approx(2 ** -0.5)
+
+
+def test_lowering_positions_follow_counter_mod_n():  # simulation.rs:37-56
+    qc = Circuit(3)
+    qc.add_gates([Gate.H, Gate.Id, Gate.Rz(0.25)]).add_gate(Gate.CNot(0), 2) \
+        .add_gate(Gate.Toffoli(2, 0), 1).add_gate(Gate.CRk(3, 1), 0)
+    prog = lower(qc.get_gates(), 3)
+    kinds = [_native.KINDS[k] for k in prog.ops["kind"]]
+    assert kinds == ["H", "Rz", "CNot", "Toffoli", "CRk"]
+    assert list(prog.ops["target"]) == [0, 2, 2, 1, 0]
+    assert list(prog.ops["n_controls"]) == [0, 0, 1, 2, 1]
+    assert prog.ops["controls"][3][:2].tolist() == [2, 0]
+    assert prog.ops["k"][4] == 3 and prog.ops["param"][1] == 0.25
+
+
+def test_custom_tabulation_columns_and_none():
+    block, none = tabulate_custom(G.example_cnot, 2)
+    assert none.tolist() == [1, 1, 0, 0]
+    assert np.array_equal(block[2], [0, 0, 0, 1]) and np.array_equal(block[3], [0, 0, 1, 0])
+    with pytest.raises(QuantrError):
+        tabulate_custom(lambda p: SuperPosition.new_with_amplitudes_unchecked([1, 0]), 2)
+
+
+def test_workloads_are_deterministic_and_api_consistent():
+    a = W.brickwork_qft(n=6, layers=3, seed=9)
+    b = W.brickwork_qft(n=6, layers=3, seed=9)
+    assert a.ops.tobytes() == b.ops.tobytes()
+    c = lower(W.brickwork_qft_circuit(6, layers=3, seed=9).get_gates(), 6)
+    assert c.ops.tobytes() == a.ops.tobytes()
+    assert len(W.brickwork_qft(n=30).ops) == 20 * 90 + sum(1 for l in range(20)
+                                                           for _ in range(l % 2, 29, 2)) + 30 + 435 + 15
+    r = W.random_columns(n=12, seed=1)
+    assert len(r.ops) > 40 * 12
+
+
+def test_op_record_layout_matches_header():
+    hdr = (ROOT / "include" / "qgpu.h").read_text()
+    assert "QGPU_MAX_OP_WIRES 10" in hdr
+    assert OP_DTYPE.itemsize == C.sizeof(_native.QgpuOp) == 80
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    """The C-ABI library loads without a GPU and exports every function of include/*.h."""
+    lib = _native.load()
+    declared = set()
+    for h in (ROOT / "include").glob("*.h"):
+        declared |= set(re.findall(r"^\s*(?:int|const char\*|uint64_t|void)\s+(qgpu_\w+)\s*\(",
+                                   h.read_text(), re.M))
+    assert "qgpu_apply_program" in declared and "qgpu_measure" in declared
+    for name in sorted(declared):
+        assert hasattr(lib, name), f"{name} not exported"
+    assert set(_native.exported_symbols()) <= declared | set()
+
+
+def test_no_oracle_in_product_package():
+    """The product package never imports or links the oracle."""
+    pat = re.compile(r"(import\s+oracle|from\s+oracle|liboracle|quantr_oracle|oracle_simulate)")
+    for p in (ROOT / "quantr_gb300").rglob("*"):
+        if p.suffix in (".py", ".cu", ".cuh", ".cpp", ".h"):
+            assert not pat.search(p.read_text()), p

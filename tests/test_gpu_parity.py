@@ -1,0 +1,310 @@
+"""GPU parity: libquantr_gpu against the oracle and the reference's own known answers.
+
+Bars (written per test):
+  * QGPU_MODE_EXACT (complex128): amplitudes equal the oracle's value for value (np.array_equal;
+    only the sign of a zero may differ).
+  * QGPU_MODE_FAST / QGPU_MODE_F64 (complex128): max |a_gpu - a_oracle| <= 1e-12.
+  * complex64: fidelity 1 - |<psi64|psi128>|^2 <= 1e-8 and max |delta a| <= 1e-5.
+  * shots: index-for-index equal to the oracle's linear-scan rule for the same uniforms, except
+    where u lies within 1e-12 of a cumulative boundary; seeded histograms pass a chi-square test
+    against the oracle's |a|^2.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from golden import quantr_goldens as G
+from quantr_gb300 import Circuit, Gate, QuantrError, SuperPosition, set_default_backend
+from quantr_gb300 import _native as nat
+from quantr_gb300 import workloads as W
+from quantr_gb300.program import ProgramBuilder, lower
+
+pytestmark = pytest.mark.gpu
+
+TOL_FAST = 1e-12
+MODES = {"exact": nat.QGPU_MODE_EXACT, "fast": nat.QGPU_MODE_FAST, "f64": nat.QGPU_MODE_F64}
+
+
+def run_gpu(prog, mode, precision=nat.QGPU_C128, reg=None):
+    h = nat.Handle(prog.n, precision, MODES[mode] if isinstance(mode, str) else mode)
+    if reg is not None:
+        h.upload(reg)
+    h.apply(prog.ops, prog.mats, prog.none)
+    out = h.download()
+    h.close()
+    return out
+
+
+@pytest.fixture(autouse=True)
+def _lib(gpu_lib):
+    yield
+    set_default_backend(precision="c128", mode="fast")
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast", "f64"])
+@pytest.mark.parametrize("case", G.AMPLITUDE_CASES, ids=[c[0] for c in G.AMPLITUDE_CASES])
+def test_reference_goldens_on_gpu(case, mode):
+    name, builder, expected, tol, cite = case
+    set_default_backend(mode=mode)
+    qc = builder()
+    out = qc.simulate().get_state().take().get_amplitudes()
+    assert np.max(np.abs(out - expected)) < tol, cite
+
+
+def test_exact_mode_equals_oracle_cfg1(oracle):
+    """12-qubit random columns (the CPU-runnable config): value-for-value equal."""
+    prog = W.random_columns(n=12, seed=1)
+    ref = oracle.simulate(prog, engine=oracle.HASHMAP)
+    out = run_gpu(prog, "exact")
+    assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_exact_mode_equals_oracle_random(oracle, seed):
+    prog = W.random_columns(n=9, columns=25, seed=seed)
+    assert np.array_equal(run_gpu(prog, "exact"), oracle.simulate(prog, engine=oracle.DENSE))
+
+
+def test_exact_mode_equals_oracle_brickwork(oracle):
+    prog = W.brickwork_qft(n=12, layers=6, seed=2)
+    assert np.array_equal(run_gpu(prog, "exact"), oracle.simulate(prog, engine=oracle.DENSE))
+
+
+def test_exact_mode_customs_equal_oracle(oracle):
+    prog = lower(G.x3sudoko_circuit().get_gates(), 10)
+    assert np.array_equal(run_gpu(prog, "exact"), oracle.simulate(prog, engine=oracle.HASHMAP))
+
+
+@pytest.mark.parametrize("mode", ["fast", "f64"])
+def test_fused_modes_within_tolerance_cfg1(oracle, mode):
+    prog = W.random_columns(n=12, seed=1)
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    assert np.max(np.abs(run_gpu(prog, mode) - ref)) <= TOL_FAST
+
+
+@pytest.mark.parametrize("mode", ["fast", "f64"])
+@pytest.mark.parametrize("n", [5, 11, 16])
+def test_fused_modes_brickwork_qft(oracle, mode, n):
+    """The 30-qubit headline family at sizes the oracle finishes in seconds."""
+    prog = W.brickwork_qft(n=n, layers=20, seed=2)
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    assert np.max(np.abs(run_gpu(prog, mode) - ref)) <= TOL_FAST
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast", "f64"])
+def test_every_gate_on_every_wire(oracle, mode):
+    """Exhaustive sweep: each gate kind on each target, controls above and below the target,
+    on a random register (bit-mask indexing must be exact for every position)."""
+    n = 6
+    rng = np.random.default_rng(5)
+    reg = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    reg /= np.linalg.norm(reg)
+    b = ProgramBuilder(n)
+    for t in range(n):
+        for name in ("H", "X", "Y", "Z", "S", "Sdag", "T", "Tdag", "X90", "Y90", "MX90", "MY90"):
+            b.add(name, t)
+        for name in ("Rx", "Ry", "Rz", "Phase"):
+            b.add(name, t, (), param=0.3 + t)
+        for c in range(n):
+            if c == t:
+                continue
+            b.add("CNot", t, (c,))
+            b.add("CY", t, (c,))
+            b.add("CZ", t, (c,))
+            b.add("Swap", t, (c,))
+            b.add("CR", t, (c,), param=0.7 * c - t)
+            b.add("CRk", t, (c,), k=1 + (c + t) % 5)
+            c2 = (c + 1 + t) % n
+            if c2 not in (c, t):
+                b.add("Toffoli", t, (c, c2))
+    prog = b.build()
+    ref = oracle.simulate(prog, reg, engine=oracle.DENSE)
+    out = run_gpu(prog, mode, reg=reg)
+    if mode == "exact":
+        assert np.array_equal(out, ref)
+    else:
+        assert np.max(np.abs(out - ref)) <= TOL_FAST
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_custom_blocks_dense_nonunitary_and_wide(oracle, mode):
+    """Custom gates: a dense 3-wire block with None entries, a non-unitary block, and the widest
+    block (QGPU_MAX_OP_WIRES = 10 wires) on a register with an unused wire."""
+    n = 11
+    rng = np.random.default_rng(3)
+    b = ProgramBuilder(n)
+    for w in range(n):
+        b.add("H", w)
+    blk = rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8))
+    b.add_custom(4, [9, 1], blk, np.array([0, 1, 0, 0, 1, 0, 0, 0], np.uint8))
+    b.add_custom(2, [], np.array([[2 ** 0.5, 0], [0, 0]], np.complex128), np.zeros(2, np.uint8))
+    d = 1 << 10
+    wide = np.eye(d, dtype=np.complex128)[rng.permutation(d)] * np.exp(1j * rng.random(d))[:, None]
+    b.add_custom(0, [10, 1, 2, 3, 4, 5, 6, 7, 8], wide, np.zeros(d, np.uint8))
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    out = run_gpu(prog, mode)
+    if mode == "exact":
+        assert np.array_equal(out, ref)
+    else:
+        assert np.max(np.abs(out - ref)) <= TOL_FAST * max(1.0, np.max(np.abs(ref)))
+
+
+def test_complex64_consistency(oracle):
+    prog = W.brickwork_qft(n=14, layers=20, seed=3)
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    out = run_gpu(prog, "fast", precision=nat.QGPU_C64)
+    fid = abs(np.vdot(ref, out)) ** 2 / (np.vdot(out, out).real * np.vdot(ref, ref).real)
+    assert 1.0 - fid <= 1e-8
+    assert np.max(np.abs(out - ref)) <= 1e-5
+
+
+def test_upload_download_roundtrip_and_reductions():
+    rng = np.random.default_rng(1)
+    n = 13
+    a = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    h = nat.Handle(n)
+    h.upload(a)
+    assert np.array_equal(h.download(), a)
+    assert h.norm() == pytest.approx(float(np.sum(np.abs(a) ** 2)), rel=1e-13)
+    assert h.checksum() == pytest.approx(complex(np.sum(a)), rel=1e-12, abs=1e-9)
+    h.set_zero()
+    z = h.download()
+    assert z[0] == 1 and np.count_nonzero(z) == 1
+    h64 = nat.Handle(n, nat.QGPU_C64)
+    h64.upload(a)
+    assert np.max(np.abs(h64.download() - a.astype(np.complex64))) == 0.0
+
+
+def test_argument_errors_are_reported():
+    h = nat.Handle(4)
+    b = ProgramBuilder(4)
+    b.add("CNot", 2, (2,))          # control equals target
+    with pytest.raises(QuantrError):
+        p = b.build()
+        h.apply(p.ops, p.mats, p.none)
+    b = ProgramBuilder(4)
+    b.add("H", 4)                   # wire out of range
+    with pytest.raises(QuantrError):
+        p = b.build()
+        h.apply(p.ops, p.mats, p.none)
+    with pytest.raises(QuantrError):
+        h.upload(np.zeros(8, np.complex128))  # wrong register size
+    with pytest.raises(QuantrError):
+        nat.Handle(40)               # 16 TiB of complex128: out of memory, reported
+    empty = ProgramBuilder(4).build()
+    h.apply(empty.ops, empty.mats, empty.none)  # empty program is a no-op
+    assert h.download()[0] == 1
+
+
+def test_single_qubit_register(oracle):
+    b = ProgramBuilder(1)
+    for name in ("H", "T", "Y", "Rx", "S"):
+        b.add(name, 0, (), param=0.9)
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    assert np.array_equal(run_gpu(prog, "exact"), ref)
+    assert np.max(np.abs(run_gpu(prog, "fast") - ref)) <= TOL_FAST
+
+
+# ---------------------------------------------------------------------------------------------
+# measurement
+# ---------------------------------------------------------------------------------------------
+def _near_boundary(state, u, tol=1e-12):
+    cum = np.cumsum(np.abs(state) ** 2)
+    j = np.searchsorted(cum, u, side="right")
+    lo = np.abs(u - cum[np.clip(j - 1, 0, cum.size - 1)])
+    hi = np.abs(u - cum[np.clip(j, 0, cum.size - 1)])
+    return np.minimum(lo, hi) < tol
+
+
+@pytest.mark.parametrize("n", [3, 7, 12, 16])
+def test_shot_rule_matches_linear_scan(oracle, n):
+    prog = W.random_columns(n=n, columns=10, seed=n)
+    state = oracle.simulate(prog, engine=oracle.DENSE)
+    h = nat.Handle(n)
+    h.upload(state)
+    rng = np.random.default_rng(n)
+    u = rng.random(20000)
+    u[:3] = [0.0, np.nextafter(1.0, 0.0), 0.5]
+    got = h.measure_uniforms(u)
+    want = oracle.measure_uniforms(state, u)
+    differ = got != want
+    assert not np.any(differ & ~_near_boundary(state, u))
+
+
+def test_shots_none_beyond_total_probability(oracle):
+    n = 5
+    state = np.full(1 << n, (0.5 / (1 << n)) ** 0.5, dtype=np.complex128)  # total 0.5
+    h = nat.Handle(n)
+    h.upload(state)
+    u = np.array([0.1, 0.49, 0.51, 0.9])
+    assert np.array_equal(h.measure_uniforms(u), oracle.measure_uniforms(state, u))
+    idx, cnt, failed = h.measure(10000, seed=3)
+    assert 4000 < failed < 6000 and cnt.sum() + failed == 10000
+
+
+def test_measure_all_chi_square(oracle):
+    scipy_stats = pytest.importorskip("scipy.stats")
+    prog = W.random_columns(n=12, seed=1)
+    state = oracle.simulate(prog, engine=oracle.DENSE)
+    h = nat.Handle(12)
+    h.upload(state)
+    shots = 200000
+    idx, cnt, failed = h.measure(shots, seed=1234)
+    assert failed == 0 and cnt.sum() == shots and np.all(np.diff(idx.astype(np.int64)) > 0)
+    obs = np.zeros(1 << 12)
+    obs[idx.astype(np.int64)] = cnt
+    exp = np.abs(state) ** 2 * shots
+    order = np.argsort(exp)
+    # merge the smallest bins until each merged bin expects >= 5
+    o_m, e_m, acc_o, acc_e = [], [], 0.0, 0.0
+    for i in order:
+        acc_o += obs[i]
+        acc_e += exp[i]
+        if acc_e >= 5:
+            o_m.append(acc_o)
+            e_m.append(acc_e)
+            acc_o = acc_e = 0.0
+    if acc_e > 0:
+        o_m[-1] += acc_o
+        e_m[-1] += acc_e
+    o_m, e_m = np.array(o_m), np.array(e_m)
+    chi2 = float(np.sum((o_m - e_m) ** 2 / e_m))
+    p = scipy_stats.chi2.sf(chi2, len(o_m) - 1)
+    assert p > 1e-4, (chi2, len(o_m))
+
+
+def test_grovers_histogram_thresholds():
+    """tests/grovers.rs:62-69: measure_all(500) finds only 011 and 111, each > 200 times."""
+    sim = G.grovers_3qubit_circuit().simulate()
+    bins = sim.measure_all(500).take()
+    for state, count in bins.items():
+        if str(state) in ("011", "111"):
+            assert count > 200
+        else:
+            assert count == 0
+
+
+def test_x3sudoko_histogram_thresholds():
+    """tests/grovers.rs:141-152: measure_all(5000) on the 10-qubit sudoku oracle."""
+    sim = G.x3sudoko_circuit().simulate()
+    sim.print_warnings(True)
+    bins = sim.measure_all(5000).take()
+    for state, count in bins.items():
+        if str(state)[:6] in G.X3SUDOKO_SOLUTIONS:
+            assert count > 150
+        else:
+            assert count < 150
+
+
+def test_measure_all_without_cache_post_select():
+    """examples/post_select.rs with per-shot re-simulation: every shot sees |x0x> outcomes."""
+    qc = Circuit(3)
+    qc.add_repeating_gate(Gate.H, [0, 1, 2]).add_gate(Gate.Custom(G.post_select, [], "P"), 1)
+    sim = qc.simulate()
+    sim.print_warnings(True)
+    bins = sim.measure_all_without_cache(20).take()
+    assert sum(bins.values()) == 20
+    assert all(str(s)[1] == "0" for s in bins)
