@@ -145,6 +145,22 @@ int qgpu_measure_uniforms(qgpu_handle* h, const double* u, size_t n, int64_t* ou
 int qgpu_norm(qgpu_handle* h, double* out);
 int qgpu_checksum(qgpu_handle* h, double* re_out, double* im_out);
 
+/* ---- engine introspection (no counterpart in quantr) ------------------------------------ */
+
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or order work on it. */
+void* qgpu_stream(qgpu_handle* h);
+/* Number of kernels this handle has launched since creation. */
+uint64_t qgpu_launch_count(const qgpu_handle* h);
+/* Bytes this handle has moved host->device (copies and kernel parameters) and device->host. */
+int qgpu_io_bytes(const qgpu_handle* h, uint64_t* h2d, uint64_t* d2h);
+/* When on, every pass of qgpu_apply_program is bracketed by CUDA events on the handle's stream
+ * and its duration and algorithmic bytes (2 * sizeof(amplitude) * amplitudes the pass may
+ * change) are accumulated per kernel. */
+int qgpu_set_profiling(qgpu_handle* h, int on);
+/* Writes the accumulated profile as JSON {"kernel": [launches, total_ms, bytes], ...} into buf
+ * (NUL-terminated, truncated to cap) and, when reset != 0, clears it. */
+int qgpu_profile_json(qgpu_handle* h, char* buf, size_t cap, int reset);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,6 +63,10 @@ _EXPORTS = {
     "qgpu_measure_uniforms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "qgpu_norm": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "qgpu_checksum": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "qgpu_stream": (C.c_void_p, [C.c_void_p]),
+    "qgpu_launch_count": (C.c_uint64, [C.c_void_p]),
+    "qgpu_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "qgpu_profile_json": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t, C.c_int]),
 }
 
 
@@ -179,3 +183,21 @@ class Handle:
         re, im = C.c_double(), C.c_double()
         check(lib().qgpu_checksum(self._h, C.byref(re), C.byref(im)), "qgpu_checksum")
         return complex(re.value, im.value)
+
+    # ---- introspection --------------------------------------------------------------------
+    def stream(self) -> int:
+        return int(lib().qgpu_stream(self._h) or 0)
+
+    def launch_count(self) -> int:
+        return int(lib().qgpu_launch_count(self._h))
+
+    def set_profiling(self, on: bool) -> None:
+        check(lib().qgpu_set_profiling(self._h, 1 if on else 0), "qgpu_set_profiling")
+
+    def profile(self, reset: bool = False) -> dict:
+        import json
+
+        buf = C.create_string_buffer(1 << 16)
+        check(lib().qgpu_profile_json(self._h, buf, len(buf), 1 if reset else 0),
+              "qgpu_profile_json")
+        return json.loads(buf.value.decode())

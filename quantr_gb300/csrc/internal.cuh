@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -54,7 +55,26 @@ struct qgpu_handle {
     qgpu::Scratch work;        // reductions, measurement buffers
     qgpu::Scratch work2;       // second buffer (measurement indices / adjoint vectors)
     uint64_t launches = 0;     // kernels launched on this handle (for benchmarking claims)
+    uint64_t h2d_bytes = 0;    // host->device traffic: copies + kernel parameter blocks
+    uint64_t d2h_bytes = 0;    // device->host copies
+    // per-pass event profiling (qgpu_set_profiling)
+    bool profile = false;
+    std::vector<cudaEvent_t> events;
+    struct ProfEntry {
+        uint64_t launches = 0;
+        double ms = 0.0;
+        double bytes = 0.0;
+    };
+    std::map<std::string, ProfEntry> prof;
 };
+
+namespace qgpu {
+// Event pair i of the handle's pool (grown on demand); nullptr when profiling is off.
+int prof_events(qgpu_handle* h, size_t pairs);
+// Reads back the recorded pairs and accumulates them under the given names.
+int prof_collect(qgpu_handle* h, const std::vector<std::string>& names,
+                 const std::vector<double>& bytes);
+}  // namespace qgpu
 
 // ---------------------------------------------------------------------------------------------
 // Index helpers. Wire w of an n-qubit register is bit (n-1-w) of the amplitude index.

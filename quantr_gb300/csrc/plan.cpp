@@ -249,6 +249,16 @@ struct HStep {
 
 int popcount64(uint64_t x) { return __builtin_popcountll(x); }
 
+// Fraction of amplitudes a step may change (its algorithmic footprint).
+double step_fraction(const HStep& h) {
+    const DevStep& s = h.s;
+    const double cond = std::ldexp(1.0, -popcount64(s.cm));
+    switch (s.type) {
+        case ST_SWAP: return 0.5;
+        default: return cond;
+    }
+}
+
 int step_cost(const HStep& h, int policy) {
     const DevStep& s = h.s;
     const int pc = popcount64(s.cm);
@@ -567,11 +577,14 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
                 if (cur_bits[m] == b) return (uint8_t)m;
             return 0;
         };
+        double touched = 0.0;
         for (HStep& h : cur_steps) {
             if (h.need[0] >= 0) h.s.lb = local(h.need[0]);
             if (h.need[1] >= 0) h.s.lb2 = local(h.need[1]);
             p.steps.push_back(h.s);
+            touched += step_fraction(h);
         }
+        p.touched = std::min(1.0, touched);
         p.arith = cur_arith;
         p.cost = cur_cost;
         plan->passes.push_back(p);

@@ -68,6 +68,7 @@ struct Pass {
     int bits[MAX_TILE_BITS];           // full-index bit positions, ascending
     bool arith = false;                // needs float-pair / f64 arithmetic
     int cost = 0;                      // planner's ops-per-amplitude estimate
+    double touched = 1.0;              // fraction of amplitudes the pass may change
     std::vector<DevStep> steps;
     int custom = -1;                   // >= 0: this pass is a Custom gate (group kernel)
 };

@@ -585,6 +585,9 @@ static int env_int(const char* name, int dflt) {
     return std::atoi(v);
 }
 
+static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, const float4* tab_ff,
+                       const double2* tab_f64, TileParams& tp);
+
 static int run_plan(qgpu_handle* h, const Plan& plan) {
     const int pol = policy_of(h);
     // phase tables for every TABLE step of the plan, uploaded once
@@ -624,12 +627,42 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         QGPU_CUDA(cudaStreamSynchronize(h->stream));
     }
     TileParams tp;
-    for (const Pass& ps : plan.passes) {
-        if (ps.custom >= 0) {
-            int st = launch_group(h, gargs[ps.custom], (const uint8_t*)h->gates.ptr, lay[ps.custom]);
-            if (st != QGPU_OK) return st;
-            continue;
+    std::vector<std::string> prof_names;
+    std::vector<double> prof_bytes;
+    if (h->profile) {
+        int st = prof_events(h, plan.passes.size());
+        if (st != QGPU_OK) return st;
+    }
+    static const char* pol_name[] = {"ff", "f64", "f32"};
+    for (size_t pi = 0; pi < plan.passes.size(); ++pi) {
+        const Pass& ps = plan.passes[pi];
+        if (h->profile) {
+            QGPU_CUDA(cudaEventRecord(h->events[2 * pi], h->stream));
+            if (ps.custom >= 0) {
+                prof_names.push_back("k_group");
+            } else {
+                prof_names.push_back(std::string("k_tile<") + std::to_string(ps.nbits) + "," +
+                                     (ps.arith ? pol_name[pol] : "move") + ">");
+            }
+            prof_bytes.push_back(2.0 * (double)h->amp_bytes * (double)h->dim * ps.touched);
         }
+        int st = QGPU_OK;
+        if (ps.custom >= 0) {
+            st = launch_group(h, gargs[ps.custom], (const uint8_t*)h->gates.ptr, lay[ps.custom]);
+        } else {
+            st = launch_pass(h, ps, pol, tab_ff, tab_f64, tp);
+        }
+        if (st != QGPU_OK) return st;
+        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * pi + 1], h->stream));
+    }
+    if (h->profile) return prof_collect(h, prof_names, prof_bytes);
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    return QGPU_OK;
+}
+
+static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, const float4* tab_ff,
+                       const double2* tab_f64, TileParams& tp) {
+    {
         std::memset(&tp, 0, sizeof(tp));
         tp.nbits = ps.nbits;
         for (int m = 0; m < ps.nbits; ++m) tp.bits[m] = ps.bits[m];
@@ -649,10 +682,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         } else {
             st = launch_tile_k<PolFF>(h, tp);
         }
-        if (st != QGPU_OK) return st;
+        return st;
     }
-    QGPU_CUDA(cudaStreamSynchronize(h->stream));
-    return QGPU_OK;
 }
 
 PlanOptions plan_options_for(const qgpu_handle* h) {

@@ -170,6 +170,29 @@ int reduce_state(qgpu_handle* h, int what, double2* host_out) {
     return QGPU_OK;
 }
 
+int prof_events(qgpu_handle* h, size_t pairs) {
+    while (h->events.size() < 2 * pairs) {
+        cudaEvent_t e;
+        QGPU_CUDA(cudaEventCreate(&e));
+        h->events.push_back(e);
+    }
+    return QGPU_OK;
+}
+
+int prof_collect(qgpu_handle* h, const std::vector<std::string>& names,
+                 const std::vector<double>& bytes) {
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < names.size(); ++i) {
+        float ms = 0.f;
+        QGPU_CUDA(cudaEventElapsedTime(&ms, h->events[2 * i], h->events[2 * i + 1]));
+        qgpu_handle::ProfEntry& e = h->prof[names[i]];
+        e.launches += 1;
+        e.ms += ms;
+        e.bytes += bytes[i];
+    }
+    return QGPU_OK;
+}
+
 }  // namespace qgpu
 
 using namespace qgpu;
@@ -177,6 +200,41 @@ using namespace qgpu;
 // ---------------------------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------------------------
+extern "C" {
+
+void* qgpu_stream(qgpu_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+uint64_t qgpu_launch_count(const qgpu_handle* h) { return h ? h->launches : 0; }
+
+int qgpu_set_profiling(qgpu_handle* h, int on) {
+    if (!h) return fail(QGPU_ERR_INVALID, "qgpu_set_profiling: NULL handle");
+    h->profile = on != 0;
+    return QGPU_OK;
+}
+
+int qgpu_profile_json(qgpu_handle* h, char* buf, size_t cap, int reset) {
+    if (!h || (!buf && cap)) return fail(QGPU_ERR_INVALID, "qgpu_profile_json: NULL argument");
+    std::string s = "{";
+    bool first = true;
+    for (const auto& kv : h->prof) {
+        char tmp[256];
+        snprintf(tmp, sizeof(tmp), "%s\"%s\": [%llu, %.6f, %.1f]", first ? "" : ", ",
+                 kv.first.c_str(), (unsigned long long)kv.second.launches, kv.second.ms,
+                 kv.second.bytes);
+        s += tmp;
+        first = false;
+    }
+    s += "}";
+    if (cap) {
+        const size_t n = s.size() < cap - 1 ? s.size() : cap - 1;
+        memcpy(buf, s.data(), n);
+        buf[n] = 0;
+    }
+    if (reset) h->prof.clear();
+    return QGPU_OK;
+}
+
+}  // extern "C"
 extern "C" {
 
 const char* qgpu_last_error(void) { return g_last_error.c_str(); }
@@ -240,6 +298,7 @@ int qgpu_destroy(qgpu_handle* h) {
     h->gates.release();
     h->work.release();
     h->work2.release();
+    for (cudaEvent_t e : h->events) cudaEventDestroy(e);
     if (h->state) cudaFree(h->state);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;

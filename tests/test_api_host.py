@@ -133,7 +133,7 @@ def test_library_loads_and_exports_every_declared_symbol():
     lib = _native.load()
     declared = set()
     for h in (ROOT / "include").glob("*.h"):
-        declared |= set(re.findall(r"^\s*(?:int|const char\*|uint64_t|void)\s+(qgpu_\w+)\s*\(",
+        declared |= set(re.findall(r"^\s*(?:int|const char\s*\*|uint64_t|void\s*\*?)\s*(qgpu_\w+)\s*\(",
                                    h.read_text(), re.M))
     assert "qgpu_apply_program" in declared and "qgpu_measure" in declared
     for name in sorted(declared):
