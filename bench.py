@@ -1,0 +1,352 @@
+#!/usr/bin/env python3
+"""Benchmark: 30-qubit complex128 brickwork + QFT circuit, gate application on one GB300.
+
+Workload (the metric's configuration): 20 brickwork layers of Rz(a) Ry(b) Rz(c) on every wire plus
+alternating CNot(i -> i+1) pairs, then a 30-qubit QFT (H + CRk(k) in quantr's examples/qft.rs
+pattern, then wire swaps): 2 580 gates on a 16 GiB complex128 state, seeded synthetic angles.
+
+A step = one `Circuit::simulate` of that circuit from |0...0> on a device-resident register
+(set_zero + qgpu_apply_program), timed with CUDA events on the library's stream. The 16 GiB state
+is larger than L2 (129 MB), so no flush is needed between steps.
+
+Units (GB/s):
+  value       gate-apply bytes per second: each gate counts 2 * 16 B * T_gate, where T_gate is the
+              amplitudes it may change (2^n for H/X/Y/rotations/Phase/Custom, 2^(n-1) for
+              S/T/Z/CNot/CY/Swap, 2^(n-2) for CZ/CR/CRk/Toffoli) - the bytes a gate-by-gate
+              simulator such as quantr moves. Gate fusion moves fewer bytes than this, so value
+              can exceed the HBM peak.
+  pct_peak    bytes the engine's passes actually move (2 * 16 B * amplitudes each pass may
+              change) per second, over the measured HBM peak.
+  roofline    the dominant kernel: its per-launch algorithmic bytes / its average CUDA-event
+              duration, against the measured HBM peak (MEASURED_PEAKS.json).
+  e2e         the same gate-apply GB/s through the public API (Circuit.simulate + measure_all of
+              10^6 shots + norm), program upload and histogram download inside the timed region.
+
+--impl reference times the restated reference (the oracle's HashMap engine, a port of
+src/circuit/simulation.rs: the Rust crate itself cannot be built without a Rust toolchain) on the
+host cores, on a bounded sample of the same family, in the same unit.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "30q c128 gate-apply HBM GB/s (% peak); adjoint grads/s vs plain at 1e-7"
+UNIT = "GB/s"
+FULL = {"H", "X", "Y", "Rx", "Ry", "Rz", "Phase", "X90", "Y90", "MX90", "MY90", "Custom"}
+HALF = {"Z", "S", "Sdag", "T", "Tdag", "CNot", "CY", "Swap"}
+QUARTER = {"CZ", "CR", "CRk", "Toffoli"}
+
+
+def gate_bytes(prog, amp_bytes: int = 16) -> float:
+    from quantr_gb300._native import KINDS
+
+    dim = float(1 << prog.n)
+    total = 0.0
+    for k in prog.ops["kind"]:
+        name = KINDS[int(k)]
+        frac = 1.0 if name in FULL else 0.5 if name in HALF else 0.25 if name in QUARTER else 0.0
+        total += 2.0 * amp_bytes * dim * frac
+    return total
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i in range(4) if r[i].lower() == "active"})
+        load = [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_reference_sample(n: int, budget_s: float, seed: int = 2) -> dict:
+    """The restated reference (oracle HashMap engine, single thread) on the first gates of the
+    same brickwork + QFT family at n qubits, run until budget_s elapses."""
+    from oracle import oracle as orc
+    from quantr_gb300 import workloads as W
+    from quantr_gb300.program import Program
+
+    prog = W.brickwork_qft(n=n, layers=20, seed=seed)
+    state = np.zeros(1 << n, dtype=np.complex128)
+    state[0] = 1.0
+    done_bytes = 0.0
+    gates = 0
+    chunk = 16
+    t0 = time.perf_counter()
+    while gates < len(prog.ops) and time.perf_counter() - t0 < budget_s:
+        sub = Program(n, prog.ops[gates:gates + chunk], prog.mats, prog.none)
+        state = orc.simulate(sub, state, engine=orc.HASHMAP)
+        done_bytes += gate_bytes(sub)
+        gates += len(sub.ops)
+    dt = time.perf_counter() - t0
+    return {"value": done_bytes / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"first {gates} of {len(prog.ops)} gates of the same brickwork+QFT family at "
+                      f"{n} qubits (restated reference HashMap engine, 1 thread, {dt:.1f} s)",
+            "seconds": dt, "gates": gates}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args) -> None:
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    n = args.ref_n
+    for _ in range(args.warmup):
+        cpu_reference_sample(n, budget_s=0.5)
+    vals = []
+    samples = []
+    for _ in range(args.steps):
+        s = cpu_reference_sample(n, budget_s=args.ref_budget)
+        vals.append(s["value"])
+        samples.append(s)
+    v = statistics.median(vals)
+    total_s = sum(s["seconds"] for s in samples)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_s / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"brickwork+QFT {args.n}q c128 family, bounded sample at {n} qubits",
+                   "qubits": n, "layers": 20, "seed": 2},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": samples[-1]["sample"]},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+
+    from quantr_gb300 import Circuit, _native as nat
+    from quantr_gb300 import workloads as W
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    precision = nat.QGPU_C64 if args.precision == "c64" else nat.QGPU_C128
+    amp_bytes = 8 if precision == nat.QGPU_C64 else 16
+    mode = {"fast": nat.QGPU_MODE_FAST, "f64": nat.QGPU_MODE_F64, "exact": nat.QGPU_MODE_EXACT}[args.mode]
+    prog = W.brickwork_qft(n=args.n, layers=args.layers, seed=2)
+    gbytes = gate_bytes(prog, amp_bytes)
+
+    h = nat.Handle(args.n, precision, mode)
+    stream = torch.cuda.ExternalStream(h.stream(), device=dev)
+    for _ in range(args.warmup):
+        h.set_zero()
+        h.apply(prog.ops, prog.mats, prog.none)
+    h.set_profiling(True)
+    h.profile(reset=True)
+    launches0 = h.launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            h.set_zero()
+            h.apply(prog.ops, prog.mats, prog.none)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    launches = h.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    prof = h.profile(reset=True)
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = gbytes * world / (ms_max / 1e3) / 1e9
+    pass_bytes = sum(v[2] for v in prof.values()) / args.steps
+    norm = h.norm()
+    checksum = h.checksum()
+    h.close()
+
+    peaks = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_launches, dom_ms, dom_bytes) = dom
+    achieved = (dom_bytes / dom_launches) / (dom_ms / dom_launches / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        tj = json.loads(tf.read_text())
+        kt = tj.get(f"{args.precision}:{dom_name}")
+        if kt:
+            traffic = kt["dram_bytes_per_amplitude"] * (1 << args.n)
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "peak_source": peaks["source"], "launches_per_step": dom_launches / args.steps,
+                "share_of_step": dom_ms / args.steps / ms}
+    kernels = {k: {"launches_per_step": v[0] / args.steps, "ms_per_step": v[1] / args.steps,
+                   "GBps": (v[2] / (v[1] / 1e3) / 1e9) if v[1] > 0 else None}
+               for k, v in prof.items()}
+
+    # ---- end to end through the public API -------------------------------------------------
+    e2e = None
+    if not args.no_e2e:
+        qc = W.brickwork_qft_circuit(args.n, layers=args.layers, seed=2)
+        qc.set_backend(precision=args.precision, mode=args.mode)
+        sim = qc.clone_and_simulate()
+        sim.print_warnings(True)
+        sim.measure_all(args.shots)
+        del sim
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        io = [0, 0]
+        for _ in range(args.e2e_steps):
+            sim = qc.clone_and_simulate()
+            sim.print_warnings(True)
+            bins = sim.measure_all(args.shots).take()
+            nrm = sim.handle.norm()
+            a, b = sim.handle.io_bytes()
+            io[0] += a
+            io[1] += b
+            sim.handle.close()
+            del sim
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        t = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+        e2e = {"value": gbytes * world / (e2e_ms / 1e3) / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": io[0] // args.e2e_steps,
+               "d2h_bytes_per_step": io[1] // args.e2e_steps,
+               "ms_per_step": e2e_ms, "shots": args.shots, "timer": "host wall clock",
+               "distinct_outcomes": len(bins), "norm": nrm}
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_reference_sample(args.ref_n, budget_s=args.ref_budget)
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": ("c128 state; f64 arithmetic as float pairs on FP32/INT pipes" if args.mode == "fast"
+                  and precision == nat.QGPU_C128 else f"{args.precision}/{args.mode}"),
+        "data": "synthetic (seeded SplitMix64 angles)",
+        "config": {"workload": f"brickwork+QFT {args.n}q {args.precision}: {args.layers} layers "
+                               f"Rz Ry Rz + CNot bricks, {args.n}-qubit QFT + swaps",
+                   "qubits": args.n, "gates": int(len(prog.ops)), "mode": args.mode,
+                   "parallelism": f"replicas x{world}", "l2": "state 16 GiB > L2, no flush"},
+        "pct_peak": (pass_bytes / (ms_max / 1e3) / 1e9) / peaks["hbm_gbs"],
+        "gates_per_s": len(prog.ops) / (ms_max / 1e3),
+        "roofline": roofline, "kernels": kernels,
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "result": {"norm": norm, "checksum": [checksum.real, checksum.imag]},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=30)
+    ap.add_argument("--layers", type=int, default=20)
+    ap.add_argument("--mode", choices=["fast", "f64", "exact"], default="fast")
+    ap.add_argument("--precision", choices=["c128", "c64"], default="c128")
+    ap.add_argument("--shots", type=int, default=10 ** 6)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-n", type=int, default=14)
+    ap.add_argument("--ref-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -145,6 +145,23 @@ int qgpu_measure_uniforms(qgpu_handle* h, const double* u, size_t n, int64_t* ou
 int qgpu_norm(qgpu_handle* h, double* out);
 int qgpu_checksum(qgpu_handle* h, double* re_out, double* im_out);
 
+/* ---- differentiation (no counterpart in quantr) ------------------------------------------
+ * Observable H = sum_i a[i] Z_i Z_{(i+1) mod n} + sum_i b[i] X_i over the n wires (periodic),
+ * a and b of length n. complex128 handles only. */
+
+/* <psi|H|psi> of the current register. */
+int qgpu_expectation_zzx(qgpu_handle* h, const double* a, const double* b, double* energy);
+
+/* Runs ops on the current register (leaving |psi_L> in it, like qgpu_apply_program), returns
+ * E = <psi_L|H|psi_L> and dE/dtheta for every op by the adjoint method: grads[g] is the
+ * derivative with respect to the angle of op g when it is Rx, Ry, Rz or Phase, else 0.
+ * Circuits with Custom gates are rejected with QGPU_ERR_NONUNITARY (their maps need not be
+ * invertible). Uses two state-sized work vectors. */
+int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
+                      const double* mats, size_t n_mat_doubles,
+                      const uint8_t* none_flags, size_t n_none_flags,
+                      const double* a, const double* b, double* energy, double* grads);
+
 /* ---- engine introspection (no counterpart in quantr) ------------------------------------ */
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or order work on it. */

@@ -63,8 +63,13 @@ _EXPORTS = {
     "qgpu_measure_uniforms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "qgpu_norm": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "qgpu_checksum": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "qgpu_expectation_zzx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "qgpu_adjoint_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
+                                    C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
+                                    C.POINTER(C.c_double), C.c_void_p]),
     "qgpu_stream": (C.c_void_p, [C.c_void_p]),
     "qgpu_launch_count": (C.c_uint64, [C.c_void_p]),
+    "qgpu_io_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "qgpu_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "qgpu_profile_json": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t, C.c_int]),
 }
@@ -184,12 +189,36 @@ class Handle:
         check(lib().qgpu_checksum(self._h, C.byref(re), C.byref(im)), "qgpu_checksum")
         return complex(re.value, im.value)
 
+    # ---- differentiation --------------------------------------------------------------------
+    def expectation_zzx(self, a: np.ndarray, b: np.ndarray) -> float:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        e = C.c_double()
+        check(lib().qgpu_expectation_zzx(self._h, ptr(a), ptr(b), C.byref(e)),
+              "qgpu_expectation_zzx")
+        return e.value
+
+    def adjoint_grad(self, ops, mats, none, a: np.ndarray, b: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        g = np.zeros(len(ops), dtype=np.float64)
+        e = C.c_double()
+        check(lib().qgpu_adjoint_grad(self._h, ptr(ops), len(ops), ptr(mats), mats.size, ptr(none),
+                                      none.size, ptr(a), ptr(b), C.byref(e), ptr(g)),
+              "qgpu_adjoint_grad")
+        return e.value, g
+
     # ---- introspection --------------------------------------------------------------------
     def stream(self) -> int:
         return int(lib().qgpu_stream(self._h) or 0)
 
     def launch_count(self) -> int:
         return int(lib().qgpu_launch_count(self._h))
+
+    def io_bytes(self) -> tuple[int, int]:
+        a, b = C.c_uint64(), C.c_uint64()
+        check(lib().qgpu_io_bytes(self._h, C.byref(a), C.byref(b)), "qgpu_io_bytes")
+        return int(a.value), int(b.value)
 
     def set_profiling(self, on: bool) -> None:
         check(lib().qgpu_set_profiling(self._h, 1 if on else 0), "qgpu_set_profiling")

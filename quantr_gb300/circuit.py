@@ -9,6 +9,7 @@ program and runs it on a device-resident state; the amplitudes stay in HBM until
 from __future__ import annotations
 
 import sys
+from collections.abc import Mapping
 
 import numpy as np
 
@@ -31,6 +32,36 @@ def set_default_backend(precision: str | None = None, mode: str | None = None) -
         _DEFAULTS["precision"] = _PRECISION[precision]
     if mode is not None:
         _DEFAULTS["mode"] = _MODE[mode]
+
+
+class Histogram(Mapping):
+    """`HashMap<ProductState, usize>` of `measure_all`, backed by the sampler's sorted arrays:
+    keys are materialised as `ProductState`s only when accessed."""
+
+    def __init__(self, indices: np.ndarray, counts: np.ndarray, n: int):
+        self.indices = np.asarray(indices, dtype=np.uint64)
+        self.counts = np.asarray(counts, dtype=np.uint64)
+        self.n = n
+
+    def __len__(self) -> int:
+        return int(self.indices.size)
+
+    def __iter__(self):
+        for i in self.indices:
+            yield ProductState.binary_basis(int(i), self.n)
+
+    def __getitem__(self, key: ProductState) -> int:
+        j = np.searchsorted(self.indices, np.uint64(key.comp_basis()))
+        if j < self.indices.size and int(self.indices[j]) == key.comp_basis():
+            return int(self.counts[j])
+        raise KeyError(key)
+
+    def items(self):
+        for i, c in zip(self.indices, self.counts):
+            yield ProductState.binary_basis(int(i), self.n), int(c)
+
+    def total(self) -> int:
+        return int(self.counts.sum())
 
 
 class Measurement:
@@ -256,8 +287,7 @@ class SimulatedCircuit:
         if failed and not self.disable_warnings:
             for _ in range(failed):
                 print(_WARN_NONE, file=sys.stderr)
-        bins = {ProductState.binary_basis(int(i), self.num_qubits): int(c) for i, c in zip(idx, cnt)}
-        return Observable(bins)
+        return Observable(Histogram(idx, cnt, self.num_qubits))
 
     def measure_all_without_cache(self, shots: int) -> Observable:  # simulated_circuit.rs:81-114
         """Shot 1 uses the cached register; every later shot re-simulates from |0...0>."""

@@ -1,0 +1,322 @@
+// adjoint.cu — energies <psi|H|psi> and adjoint-method gradients (no counterpart in quantr).
+//
+// H = sum_i a_i Z_i Z_{(i+1) mod n} + sum_i b_i X_i on wires i (wire i = index bit n-1-i).
+// Gradient by the adjoint method (Jones & Gacon 2020, arXiv:2009.02823): after the forward pass
+// |psi_L> = U_L ... U_1 |psi_0>, set phi = psi_L, lambda = H psi_L and walk the gates backwards.
+// For a rotation U_l = exp(-i theta P / 2) (quantr's Rx, Ry, Rz; P = X, Y, Z) the derivative is
+// dE/dtheta_l = 2 Re <lambda_l| dU_l |psi_{l-1}> = Im <lambda_l| P |phi_l>, read from the two
+// vectors before the gate is undone; Phase(theta) = exp(i theta / 2) I gives -Im <lambda|phi>.
+// Then phi <- U_l^dagger phi and lambda <- U_l^dagger lambda. One fused kernel (k_adj_1q) does
+// the gradient term and both updates of a single-wire gate in one pass; multi-wire gates are
+// undone with the fused gate passes of program.cu on each vector. All arithmetic here is f64.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+#include "plan.h"
+
+namespace qgpu {
+
+int apply_ops_on(qgpu_handle* h, void* buffer, const qgpu_op* ops, size_t n_ops);  // program.cu
+PlanOptions plan_options_for(const qgpu_handle* h);
+
+constexpr int ADJ_THREADS = 256;
+constexpr int MAX_HAM_QUBITS = 40;
+
+struct Ham {
+    int n;
+    double a[MAX_HAM_QUBITS];
+    double b[MAX_HAM_QUBITS];
+};
+
+// lambda = H psi, and per-block partial sums of Re(conj(psi) lambda)
+__global__ void __launch_bounds__(ADJ_THREADS)
+k_apply_zzx(const double2* __restrict__ psi, double2* __restrict__ lam, uint64_t dim,
+            const __grid_constant__ Ham H, double* __restrict__ partial) {
+    __shared__ double sh[ADJ_THREADS];
+    double acc = 0.0;
+    const int n = H.n;
+    for (uint64_t x = blockIdx.x * (uint64_t)ADJ_THREADS + threadIdx.x; x < dim;
+         x += (uint64_t)gridDim.x * ADJ_THREADS) {
+        double d = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const int j = (i + 1) % n;
+            const uint64_t p = ((x >> (n - 1 - i)) ^ (x >> (n - 1 - j))) & 1ull;
+            d += p ? -H.a[i] : H.a[i];
+        }
+        const double2 v = psi[x];
+        double re = d * v.x, im = d * v.y;
+        for (int i = 0; i < n; ++i) {
+            const double2 w = psi[x ^ (1ull << (n - 1 - i))];
+            re = fma(H.b[i], w.x, re);
+            im = fma(H.b[i], w.y, im);
+        }
+        lam[x] = make_double2(re, im);
+        acc = fma(v.x, re, fma(v.y, im, acc));
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = ADJ_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// One single-wire gate of the reverse sweep on bit t: optional gradient term (generator code
+// gen: 0 none, 1 X, 2 Y, 3 Z, 4 identity with sign -1), then phi, lambda <- V (phi, lambda)
+// with V = U^dagger given row-major as v[0..7] = (v00, v01, v10, v11) complex.
+struct AdjStep {
+    int t;
+    int gen;
+    double v[8];
+};
+
+__global__ void __launch_bounds__(ADJ_THREADS)
+k_adj_1q(double2* __restrict__ phi, double2* __restrict__ lam, uint64_t npairs,
+         const AdjStep s, double* __restrict__ partial) {
+    __shared__ double sh[ADJ_THREADS];
+    double acc = 0.0;
+    for (uint64_t p = blockIdx.x * (uint64_t)ADJ_THREADS + threadIdx.x; p < npairs;
+         p += (uint64_t)gridDim.x * ADJ_THREADS) {
+        const uint64_t i0 = insert_zero(p, s.t), i1 = i0 | (1ull << s.t);
+        const double2 f0 = phi[i0], f1 = phi[i1], l0 = lam[i0], l1 = lam[i1];
+        // Im(conj(l) * f) = l.x f.y - l.y f.x ; Re(conj(l) * f) = l.x f.x + l.y f.y
+        switch (s.gen) {
+            case 1:  // X
+                acc += (l0.x * f1.y - l0.y * f1.x) + (l1.x * f0.y - l1.y * f0.x);
+                break;
+            case 2:  // Y: Im(conj(l0)(-i f1) + conj(l1)(i f0)) = -Re(conj(l0) f1) + Re(conj(l1) f0)
+                acc += -(l0.x * f1.x + l0.y * f1.y) + (l1.x * f0.x + l1.y * f0.y);
+                break;
+            case 3:  // Z
+                acc += (l0.x * f0.y - l0.y * f0.x) - (l1.x * f1.y - l1.y * f1.x);
+                break;
+            case 4:  // global phase
+                acc -= (l0.x * f0.y - l0.y * f0.x) + (l1.x * f1.y - l1.y * f1.x);
+                break;
+            default:
+                break;
+        }
+        const double* v = s.v;
+        auto mv = [&](double2 a, double2 b, double2& o0, double2& o1) {
+            o0 = make_double2(v[0] * a.x - v[1] * a.y + v[2] * b.x - v[3] * b.y,
+                              v[0] * a.y + v[1] * a.x + v[2] * b.y + v[3] * b.x);
+            o1 = make_double2(v[4] * a.x - v[5] * a.y + v[6] * b.x - v[7] * b.y,
+                              v[4] * a.y + v[5] * a.x + v[6] * b.y + v[7] * b.x);
+        };
+        double2 o0, o1;
+        mv(f0, f1, o0, o1);
+        phi[i0] = o0;
+        phi[i1] = o1;
+        mv(l0, l1, o0, o1);
+        lam[i0] = o0;
+        lam[i1] = o1;
+    }
+    if (!partial) return;
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = ADJ_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// grads[g] = sum over blocks of partial[g * nb + b], for g in [0, ng)
+__global__ void k_sum_partials(const double* __restrict__ partial, int nb, int ng,
+                               double* __restrict__ out) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s += partial[(size_t)g * nb + b];
+    out[g] = s;
+}
+
+static int adj_blocks(const qgpu_handle* h, uint64_t work) {
+    uint64_t b = (work + ADJ_THREADS - 1) / ADJ_THREADS;
+    const uint64_t cap = (uint64_t)h->sm_count * 4;
+    if (b > cap) b = cap;
+    return (int)std::max<uint64_t>(1, b);
+}
+
+static bool is_rotation(int kind) {
+    return kind == QGPU_GATE_RX || kind == QGPU_GATE_RY || kind == QGPU_GATE_RZ ||
+           kind == QGPU_GATE_PHASE;
+}
+
+// The inverse of a non-Custom op as another op (U^dagger), quantr's conventions.
+static qgpu_op inverse_op(const qgpu_op& op) {
+    qgpu_op r = op;
+    switch (op.kind) {
+        case QGPU_GATE_S: r.kind = QGPU_GATE_SDAG; break;
+        case QGPU_GATE_SDAG: r.kind = QGPU_GATE_S; break;
+        case QGPU_GATE_T: r.kind = QGPU_GATE_TDAG; break;
+        case QGPU_GATE_TDAG: r.kind = QGPU_GATE_T; break;
+        case QGPU_GATE_X90: r.kind = QGPU_GATE_MX90; break;
+        case QGPU_GATE_MX90: r.kind = QGPU_GATE_X90; break;
+        case QGPU_GATE_Y90: r.kind = QGPU_GATE_MY90; break;
+        case QGPU_GATE_MY90: r.kind = QGPU_GATE_Y90; break;
+        case QGPU_GATE_RX: case QGPU_GATE_RY: case QGPU_GATE_RZ: case QGPU_GATE_PHASE:
+        case QGPU_GATE_CR:
+            r.param = -op.param;
+            break;
+        case QGPU_GATE_CRK:
+            r.kind = QGPU_GATE_CR;
+            r.param = -((2.0 * 3.14159265358979323846) / std::pow(2.0, (double)op.k));
+            break;
+        default:
+            break;  // H, X, Y, Z, CNot, CY, CZ, Swap, Toffoli are self-inverse
+    }
+    return r;
+}
+
+// Energy of the vector at `psi` into *energy; lambda = H psi left at `lam`.
+static int energy_into(qgpu_handle* h, const double2* psi, double2* lam, const Ham& H,
+                       double* partial, double* energy) {
+    const int nb = adj_blocks(h, h->dim);
+    k_apply_zzx<<<nb, ADJ_THREADS, 0, h->stream>>>(psi, lam, h->dim, H, partial);
+    QGPU_CHECK_LAUNCH("k_apply_zzx");
+    h->launches++;
+    k_sum_partials<<<1, 32, 0, h->stream>>>(partial, nb, 1, partial + nb);
+    QGPU_CHECK_LAUNCH("k_sum_partials");
+    h->launches++;
+    QGPU_CUDA(copy_async(h, energy, partial + nb, sizeof(double), cudaMemcpyDeviceToHost));
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    return QGPU_OK;
+}
+
+static int ham_from(const qgpu_handle* h, const double* a, const double* b, Ham* H) {
+    if (!a || !b) return fail(QGPU_ERR_INVALID, "observable coefficients are NULL");
+    if (h->n_qubits > MAX_HAM_QUBITS)
+        return fail(QGPU_ERR_UNSUPPORTED, "observable supports at most 40 qubits");
+    if (h->precision != QGPU_C128)
+        return fail(QGPU_ERR_UNSUPPORTED, "energies and gradients need a complex128 state");
+    std::memset(H, 0, sizeof(Ham));
+    H->n = h->n_qubits;
+    for (int i = 0; i < H->n; ++i) {
+        H->a[i] = a[i];
+        H->b[i] = b[i];
+    }
+    return QGPU_OK;
+}
+
+}  // namespace qgpu
+
+using namespace qgpu;
+
+extern "C" {
+
+int qgpu_expectation_zzx(qgpu_handle* h, const double* a, const double* b, double* energy) {
+    if (!h || !energy) return fail(QGPU_ERR_INVALID, "qgpu_expectation_zzx: NULL argument");
+    Ham H;
+    int st = ham_from(h, a, b, &H);
+    if (st != QGPU_OK) return st;
+    const int nb = adj_blocks(h, h->dim);
+    st = h->work2.ensure(h->dim * 16 + (size_t)(nb + 8) * 8 + 256);
+    if (st != QGPU_OK) return st;
+    double2* lam = (double2*)h->work2.ptr;
+    double* partial = (double*)((uint8_t*)h->work2.ptr + h->dim * 16);
+    return energy_into(h, (const double2*)h->state, lam, H, partial, energy);
+}
+
+int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double* mats,
+                      size_t n_mat_doubles, const uint8_t* none_flags, size_t n_none_flags,
+                      const double* a, const double* b, double* energy, double* grads) {
+    if (!h || !energy || !grads || (n_ops && !ops))
+        return fail(QGPU_ERR_INVALID, "qgpu_adjoint_grad: NULL argument");
+    Ham H;
+    int st = ham_from(h, a, b, &H);
+    if (st != QGPU_OK) return st;
+    for (size_t g = 0; g < n_ops; ++g) {
+        if (ops[g].kind == QGPU_GATE_CUSTOM)
+            return fail(QGPU_ERR_NONUNITARY, "adjoint gradients need invertible gates; the circuit "
+                                             "contains a Custom gate");
+        int k;
+        st = op_arity(ops[g], h->n_qubits, &k);
+        if (ops[g].kind != QGPU_GATE_ID && st != QGPU_OK) return st;
+    }
+    // forward pass on the register
+    st = qgpu_apply_program(h, ops, n_ops, mats, n_mat_doubles, none_flags, n_none_flags);
+    if (st != QGPU_OK) return st;
+    // work vectors: phi (copy of psi_L), lambda, block partials per rotation
+    size_t nrot = 0;
+    for (size_t g = 0; g < n_ops; ++g) nrot += is_rotation(ops[g].kind) ? 1 : 0;
+    const int nb = adj_blocks(h, h->dim / 2);
+    const size_t vec = h->dim * 16;
+    const size_t part_doubles = (nrot + 1) * (size_t)nb + (size_t)nrot + 64;
+    st = h->work2.ensure(2 * vec + part_doubles * 8 + 512);
+    if (st != QGPU_OK) return st;
+    double2* phi = (double2*)h->work2.ptr;
+    double2* lam = (double2*)((uint8_t*)h->work2.ptr + vec);
+    double* partial = (double*)((uint8_t*)h->work2.ptr + 2 * vec);
+    double* gsum = partial + (nrot + 1) * (size_t)nb;
+    QGPU_CUDA(cudaMemcpyAsync(phi, h->state, vec, cudaMemcpyDeviceToDevice, h->stream));
+    st = energy_into(h, phi, lam, H, partial + nrot * (size_t)nb, energy);
+    if (st != QGPU_OK) return st;
+
+    std::vector<int> rot_slot(n_ops, -1);
+    size_t slot = 0;
+    for (size_t g = 0; g < n_ops; ++g)
+        if (is_rotation(ops[g].kind)) rot_slot[g] = (int)slot++;
+    // reverse sweep
+    std::vector<qgpu_op> seg;  // consecutive multi-wire gates, undone together
+    auto flush_seg = [&]() -> int {
+        if (seg.empty()) return QGPU_OK;
+        int s2 = apply_ops_on(h, phi, seg.data(), seg.size());
+        if (s2 == QGPU_OK) s2 = apply_ops_on(h, lam, seg.data(), seg.size());
+        seg.clear();
+        return s2;
+    };
+    for (size_t gi = n_ops; gi-- > 0;) {
+        const qgpu_op& op = ops[gi];
+        if (op.kind == QGPU_GATE_ID) continue;
+        int k = 1;
+        op_arity(op, h->n_qubits, &k);
+        if (k > 1) {
+            seg.push_back(inverse_op(op));
+            continue;
+        }
+        st = flush_seg();
+        if (st != QGPU_OK) return st;
+        LocalGate lg;
+        st = tabulate(inverse_op(op), h->n_qubits, nullptr, 0, nullptr, 0, &lg);
+        if (st != QGPU_OK) return st;
+        AdjStep s;
+        s.t = h->n_qubits - 1 - op.target;
+        switch (op.kind) {
+            case QGPU_GATE_RX: s.gen = 1; break;
+            case QGPU_GATE_RY: s.gen = 2; break;
+            case QGPU_GATE_RZ: s.gen = 3; break;
+            case QGPU_GATE_PHASE: s.gen = 4; break;
+            default: s.gen = 0; break;
+        }
+        // row-major V from the column-major images: V[l][j] = M[j*2 + l]
+        for (int l = 0; l < 2; ++l)
+            for (int j = 0; j < 2; ++j) {
+                s.v[2 * (2 * l + j)] = lg.M[j * 2 + l].real();
+                s.v[2 * (2 * l + j) + 1] = lg.M[j * 2 + l].imag();
+            }
+        double* part = rot_slot[gi] >= 0 ? partial + (size_t)rot_slot[gi] * nb : nullptr;
+        k_adj_1q<<<nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, h->dim / 2, s, part);
+        QGPU_CHECK_LAUNCH("k_adj_1q");
+        h->launches++;
+    }
+    st = flush_seg();
+    if (st != QGPU_OK) return st;
+    if (nrot) {
+        k_sum_partials<<<(unsigned)((nrot + 127) / 128), 128, 0, h->stream>>>(partial, nb, (int)nrot,
+                                                                               gsum);
+        QGPU_CHECK_LAUNCH("k_sum_partials");
+        h->launches++;
+    }
+    std::vector<double> gr(nrot);
+    if (nrot) QGPU_CUDA(copy_async(h, gr.data(), gsum, nrot * 8, cudaMemcpyDeviceToHost));
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    for (size_t g = 0; g < n_ops; ++g) grads[g] = rot_slot[g] >= 0 ? gr[rot_slot[g]] : 0.0;
+    return QGPU_OK;
+}
+
+}  // extern "C"

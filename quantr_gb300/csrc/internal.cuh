@@ -50,6 +50,7 @@ struct qgpu_handle {
     uint64_t dim = 0;          // 2^n amplitudes
     size_t amp_bytes = 16;     // 16 (c128) or 8 (c64)
     void* state = nullptr;     // device amplitudes: double2[dim] or float2[dim]
+    void* active = nullptr;    // when set, gate passes run on this buffer instead of `state`
     cudaStream_t stream = nullptr;
     qgpu::Scratch gates;       // per-program device tables (custom matrices, orders, flags)
     qgpu::Scratch work;        // reductions, measurement buffers
@@ -69,6 +70,15 @@ struct qgpu_handle {
 };
 
 namespace qgpu {
+// The buffer gate passes operate on (the register, or a work vector of the adjoint sweep).
+inline void* cur_state(const qgpu_handle* h) { return h->active ? h->active : h->state; }
+// cudaMemcpyAsync on the handle's stream that also counts host<->device bytes.
+inline cudaError_t copy_async(qgpu_handle* h, void* dst, const void* src, size_t n,
+                              cudaMemcpyKind kind) {
+    if (kind == cudaMemcpyHostToDevice) h->h2d_bytes += n;
+    if (kind == cudaMemcpyDeviceToHost) h->d2h_bytes += n;
+    return cudaMemcpyAsync(dst, src, n, kind, h->stream);
+}
 // Event pair i of the handle's pool (grown on demand); nullptr when profiling is off.
 int prof_events(qgpu_handle* h, size_t pairs);
 // Reads back the recorded pairs and accumulates them under the given names.

@@ -275,10 +275,10 @@ int qgpu_measure_uniforms(qgpu_handle* h, const double* u, size_t n, int64_t* ou
     if (st != QGPU_OK) return st;
     double* du = (double*)h->work2.ptr;
     int64_t* dout = (int64_t*)((uint8_t*)h->work2.ptr + ((n * 8 + 255) / 256) * 256);
-    QGPU_CUDA(cudaMemcpyAsync(du, u, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    QGPU_CUDA(copy_async(h, du, u, n * sizeof(double), cudaMemcpyHostToDevice));
     st = run_sample(h, c, du, n, dout);
     if (st != QGPU_OK) return st;
-    QGPU_CUDA(cudaMemcpyAsync(out, dout, n * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+    QGPU_CUDA(copy_async(h, out, dout, n * sizeof(int64_t), cudaMemcpyDeviceToHost));
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
     return QGPU_OK;
 }
@@ -321,7 +321,7 @@ int qgpu_measure(qgpu_handle* h, uint64_t shots, uint64_t seed, uint64_t* idx_ou
     st = run_sample(h, c, du, shots, dout);
     if (st != QGPU_OK) return st;
     std::vector<int64_t> idx(shots);
-    QGPU_CUDA(cudaMemcpyAsync(idx.data(), dout, shots * 8, cudaMemcpyDeviceToHost, h->stream));
+    QGPU_CUDA(copy_async(h, idx.data(), dout, shots * 8, cudaMemcpyDeviceToHost));
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
     // indices are non-decreasing (sorted uniforms, monotone search); None (-1) shots come last
     size_t nu = 0;

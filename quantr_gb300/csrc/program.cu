@@ -164,11 +164,12 @@ static int launch_group(qgpu_handle* h, const GroupArgs& a0, const uint8_t* dev_
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_group)");
     }
     if (h->precision == QGPU_C128)
-        k_group<double2><<<(unsigned)blocks, 256, smem, h->stream>>>((double2*)h->state, a);
+        k_group<double2><<<(unsigned)blocks, 256, smem, h->stream>>>((double2*)cur_state(h), a);
     else
-        k_group<float2><<<(unsigned)blocks, 256, smem, h->stream>>>((float2*)h->state, a);
+        k_group<float2><<<(unsigned)blocks, 256, smem, h->stream>>>((float2*)cur_state(h), a);
     QGPU_CHECK_LAUNCH("k_group");
     h->launches++;
+    h->h2d_bytes += sizeof(GroupArgs);
     return QGPU_OK;
 }
 
@@ -189,7 +190,7 @@ static int run_groups(qgpu_handle* h, const std::vector<const LocalGate*>& gates
     }
     int st = h->gates.ensure(at);
     if (st != QGPU_OK) return st;
-    QGPU_CUDA(cudaMemcpyAsync(h->gates.ptr, host.data(), at, cudaMemcpyHostToDevice, h->stream));
+    QGPU_CUDA(copy_async(h, h->gates.ptr, host.data(), at, cudaMemcpyHostToDevice));
     for (size_t i = 0; i < gates.size(); ++i) {
         st = launch_group(h, args[i], (const uint8_t*)h->gates.ptr, lay[i]);
         if (st != QGPU_OK) return st;
@@ -559,9 +560,10 @@ static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
     const uint64_t cap = (uint64_t)h->sm_count * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    k_tile<K, U, P><<<(unsigned)blocks, 256, 0, h->stream>>>((typename P::S*)h->state, p);
+    k_tile<K, U, P><<<(unsigned)blocks, 256, 0, h->stream>>>((typename P::S*)cur_state(h), p);
     QGPU_CHECK_LAUNCH("k_tile");
     h->launches++;
+    h->h2d_bytes += sizeof(TileParams);
     return QGPU_OK;
 }
 
@@ -598,10 +600,10 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         const size_t ffb = align_up(nent * 16, 256);
         int st = h->work2.ensure(ffb + nent * 16);
         if (st != QGPU_OK) return st;
-        QGPU_CUDA(cudaMemcpyAsync(h->work2.ptr, plan.table_ff.data(), nent * 16,
-                                  cudaMemcpyHostToDevice, h->stream));
-        QGPU_CUDA(cudaMemcpyAsync((uint8_t*)h->work2.ptr + ffb, plan.table_f64.data(), nent * 16,
-                                  cudaMemcpyHostToDevice, h->stream));
+        QGPU_CUDA(copy_async(h, h->work2.ptr, plan.table_ff.data(), nent * 16,
+                             cudaMemcpyHostToDevice));
+        QGPU_CUDA(copy_async(h, (uint8_t*)h->work2.ptr + ffb, plan.table_f64.data(), nent * 16,
+                             cudaMemcpyHostToDevice));
         tab_ff = (const float4*)h->work2.ptr;
         tab_f64 = (const double2*)((uint8_t*)h->work2.ptr + ffb);
     }
@@ -623,7 +625,7 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         }
         int st = h->gates.ensure(at);
         if (st != QGPU_OK) return st;
-        QGPU_CUDA(cudaMemcpyAsync(h->gates.ptr, host.data(), at, cudaMemcpyHostToDevice, h->stream));
+        QGPU_CUDA(copy_async(h, h->gates.ptr, host.data(), at, cudaMemcpyHostToDevice));
         QGPU_CUDA(cudaStreamSynchronize(h->stream));
     }
     TileParams tp;
@@ -694,6 +696,19 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     else o.budget = env_int("QGPU_F64_BUDGET", 1 << 20);
     o.max_bits = std::max(2, std::min(env_int("QGPU_TILE_BITS", MAX_TILE_BITS), MAX_TILE_BITS));
     return o;
+}
+
+// Runs non-Custom ops as fused passes on `buffer` (a state-sized device vector of the handle's
+// precision) instead of the register.
+int apply_ops_on(qgpu_handle* h, void* buffer, const qgpu_op* ops, size_t n_ops) {
+    Plan plan;
+    int st = build_plan(ops, n_ops, h->n_qubits, nullptr, 0, nullptr, 0, plan_options_for(h), &plan);
+    if (st != QGPU_OK) return st;
+    void* saved = h->active;
+    h->active = buffer;
+    st = run_plan(h, plan);
+    h->active = saved;
+    return st;
 }
 
 }  // namespace qgpu

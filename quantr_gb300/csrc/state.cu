@@ -164,8 +164,7 @@ int reduce_state(qgpu_handle* h, int what, double2* host_out) {
     k_reduce_final<<<1, RED_THREADS, 0, h->stream>>>(partial, nb, partial + nb);
     QGPU_CHECK_LAUNCH("k_reduce_final");
     h->launches += 2;
-    QGPU_CUDA(cudaMemcpyAsync(host_out, partial + nb, sizeof(double2), cudaMemcpyDeviceToHost,
-                              h->stream));
+    QGPU_CUDA(copy_async(h, host_out, partial + nb, sizeof(double2), cudaMemcpyDeviceToHost));
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
     return QGPU_OK;
 }
@@ -205,6 +204,13 @@ extern "C" {
 void* qgpu_stream(qgpu_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 uint64_t qgpu_launch_count(const qgpu_handle* h) { return h ? h->launches : 0; }
+
+int qgpu_io_bytes(const qgpu_handle* h, uint64_t* h2d, uint64_t* d2h) {
+    if (!h || !h2d || !d2h) return fail(QGPU_ERR_INVALID, "qgpu_io_bytes: NULL argument");
+    *h2d = h->h2d_bytes;
+    *d2h = h->d2h_bytes;
+    return QGPU_OK;
+}
 
 int qgpu_set_profiling(qgpu_handle* h, int on) {
     if (!h) return fail(QGPU_ERR_INVALID, "qgpu_set_profiling: NULL handle");
@@ -337,8 +343,7 @@ int qgpu_upload(qgpu_handle* h, const double* interleaved, size_t n_amplitudes) 
                         " amplitudes but the circuit has " + std::to_string(h->dim) +
                         " (2^" + std::to_string(h->n_qubits) + ")");
     if (h->precision == QGPU_C128) {
-        QGPU_CUDA(cudaMemcpyAsync(h->state, interleaved, h->dim * 16, cudaMemcpyHostToDevice,
-                                  h->stream));
+        QGPU_CUDA(copy_async(h, h->state, interleaved, h->dim * 16, cudaMemcpyHostToDevice));
         QGPU_CUDA(cudaStreamSynchronize(h->stream));
         return QGPU_OK;
     }
@@ -348,8 +353,8 @@ int qgpu_upload(qgpu_handle* h, const double* interleaved, size_t n_amplitudes) 
     if (st != QGPU_OK) return st;
     for (uint64_t off = 0; off < h->dim; off += stage) {
         const uint64_t cnt = (h->dim - off) < stage ? (h->dim - off) : stage;
-        QGPU_CUDA(cudaMemcpyAsync(h->work.ptr, interleaved + 2 * off, cnt * 16,
-                                  cudaMemcpyHostToDevice, h->stream));
+        QGPU_CUDA(copy_async(h, h->work.ptr, interleaved + 2 * off, cnt * 16,
+                             cudaMemcpyHostToDevice));
         k_d2f<<<grid_for(h, cnt, 256), 256, 0, h->stream>>>((const double2*)h->work.ptr,
                                                             (float2*)h->state + off, cnt);
         QGPU_CHECK_LAUNCH("k_d2f");
@@ -366,7 +371,7 @@ int qgpu_download(qgpu_handle* h, double* out, size_t n_amplitudes) {
                                           std::to_string(n_amplitudes) + " amplitudes, need " +
                                           std::to_string(h->dim));
     if (h->precision == QGPU_C128) {
-        QGPU_CUDA(cudaMemcpyAsync(out, h->state, h->dim * 16, cudaMemcpyDeviceToHost, h->stream));
+        QGPU_CUDA(copy_async(h, out, h->state, h->dim * 16, cudaMemcpyDeviceToHost));
         QGPU_CUDA(cudaStreamSynchronize(h->stream));
         return QGPU_OK;
     }
@@ -380,8 +385,7 @@ int qgpu_download(qgpu_handle* h, double* out, size_t n_amplitudes) {
                                                             (double2*)h->work.ptr, cnt);
         QGPU_CHECK_LAUNCH("k_f2d");
         h->launches++;
-        QGPU_CUDA(cudaMemcpyAsync(out + 2 * off, h->work.ptr, cnt * 16, cudaMemcpyDeviceToHost,
-                                  h->stream));
+        QGPU_CUDA(copy_async(h, out + 2 * off, h->work.ptr, cnt * 16, cudaMemcpyDeviceToHost));
     }
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
     return QGPU_OK;

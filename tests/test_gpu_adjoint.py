@@ -1,0 +1,97 @@
+"""Adjoint gradients (config: 20-qubit hardware-efficient ansatz, 400 parameters).
+
+Bars: max |g_adjoint - g_FD| <= 1e-7 (central differences, h = 1e-6) and
+max |g_adjoint - g_shift| <= 1e-9 (parameter shift +-pi/2), complex128. Small cases also check
+against the CPU oracle with numpy finite differences.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from quantr_gb300 import QuantrError
+from quantr_gb300 import _native as nat
+from quantr_gb300 import gradients as GR
+from quantr_gb300 import workloads as W
+from quantr_gb300.program import ProgramBuilder, Program
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _lib(gpu_lib):
+    yield
+
+
+def _oracle_energy(orc, prog, a, b):
+    return W.energy_dense(orc.simulate(prog, engine=orc.DENSE), a, b)
+
+
+def _oracle_fd(orc, prog, a, b, h=1e-6):
+    g = np.zeros(len(prog.ops))
+    for i, k in enumerate(prog.ops["kind"]):
+        if int(k) in GR.ROTATIONS:
+            up = prog.ops.copy()
+            up["param"][i] += h
+            dn = prog.ops.copy()
+            dn["param"][i] -= h
+            g[i] = (_oracle_energy(orc, Program(prog.n, up, prog.mats, prog.none), a, b)
+                    - _oracle_energy(orc, Program(prog.n, dn, prog.mats, prog.none), a, b)) / (2 * h)
+    return g
+
+
+def test_energy_matches_oracle(oracle):
+    an = W.ansatz(n=8, layers=3, seed=4)
+    prog = an.program()
+    h = nat.Handle(8)
+    e = GR.energy(h, prog, an.a, an.b)
+    assert e == pytest.approx(_oracle_energy(oracle, prog, an.a, an.b), abs=1e-12)
+
+
+def test_adjoint_all_gate_kinds_vs_oracle_fd(oracle):
+    """Every invertible gate kind in the circuit (the sweep undoes each one)."""
+    n = 6
+    rng = np.random.default_rng(0)
+    b = ProgramBuilder(n)
+    for layer in range(2):
+        for w in range(n):
+            b.add(["Rx", "Ry", "Rz", "Phase"][(w + layer) % 4], w, (), param=rng.uniform(-3, 3))
+        b.add("H", 0); b.add("S", 1); b.add("T", 2); b.add("Sdag", 3); b.add("Tdag", 4)
+        b.add("X90", 5); b.add("Y90", 0); b.add("MX90", 1); b.add("MY90", 2); b.add("Y", 3)
+        b.add("CNot", 1, (0,)); b.add("CZ", 2, (4,)); b.add("CY", 5, (3,)); b.add("Swap", 0, (5,))
+        b.add("CR", 3, (1,), param=0.37); b.add("CRk", 4, (2,), k=3); b.add("Toffoli", 1, (3, 5))
+        for w in range(n):
+            b.add("Ry", w, (), param=rng.uniform(-3, 3))
+    prog = b.build()
+    a_c = rng.normal(size=n)
+    b_c = rng.normal(size=n)
+    h = nat.Handle(n)
+    e, g = GR.energy_and_gradient(h, prog, a_c, b_c)
+    assert e == pytest.approx(_oracle_energy(oracle, prog, a_c, b_c), abs=1e-12)
+    fd = _oracle_fd(oracle, prog, a_c, b_c)
+    assert np.max(np.abs(g - fd)) <= 1e-7
+
+
+def test_adjoint_ansatz_20q_vs_fd_and_parameter_shift():
+    """The differentiation config: 20 qubits, 10 layers of Ry Rz + CNot ring, 400 parameters."""
+    an = W.ansatz(n=20, layers=10, seed=4)
+    prog = an.program()
+    h = nat.Handle(20)
+    e, g = GR.energy_and_gradient(h, prog, an.a, an.b)
+    rot = np.isin(prog.ops["kind"], list(GR.ROTATIONS))
+    assert rot.sum() == 400
+    fd = GR.finite_difference(h, prog, an.a, an.b, h=1e-6)
+    ps = GR.parameter_shift(h, prog, an.a, an.b)
+    assert np.max(np.abs(g - fd)) <= 1e-7
+    assert np.max(np.abs(g - ps)) <= 1e-9
+    assert math.isfinite(e)
+
+
+def test_adjoint_rejects_custom():
+    b = ProgramBuilder(3)
+    b.add("H", 0)
+    b.add_custom(1, [0], np.eye(4, dtype=np.complex128), np.zeros(4, np.uint8))
+    prog = b.build()
+    h = nat.Handle(3)
+    with pytest.raises(QuantrError):
+        h.adjoint_grad(prog.ops, prog.mats, prog.none, np.ones(3), np.ones(3))
