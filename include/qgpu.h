@@ -141,6 +141,17 @@ int qgpu_measure(qgpu_handle* h, uint64_t shots, uint64_t seed,
  * drawn for u[i], or -1 for `None`. Used to check the sampler shot by shot. */
 int qgpu_measure_uniforms(qgpu_handle* h, const double* u, size_t n, int64_t* out);
 
+/* No counterpart in quantr. qgpu_measure_uniforms for callers that cannot let the library
+ * allocate device memory (all of the GPU's memory owned by a host framework's pool, or a loop
+ * that must not enter the CUDA allocator): same arguments and results, but its scratch lives
+ * in a fixed array inside the library's device image (about 1.5 MiB, held by every GPU that
+ * loads the library until exit) and it calls no cudaMalloc/cudaFree. Limits: registers of at
+ * most 24 qubits and at most 65536 uniforms per call; larger requests fail with
+ * QGPU_ERR_INVALID. The first call on each device looks up the array's device address, so make
+ * that call before any stream capture. All calls share the one array: calls that overlap on
+ * the GPU (other handles' streams on the same device) race. */
+int qgpu_measure_uniforms_noalloc(qgpu_handle* h, const double* u, size_t n, int64_t* out);
+
 /* f64 reductions of the state: sum |a_i|^2, and the amplitude checksum sum a_i. */
 int qgpu_norm(qgpu_handle* h, double* out);
 int qgpu_checksum(qgpu_handle* h, double* re_out, double* im_out);

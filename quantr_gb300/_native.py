@@ -61,6 +61,7 @@ _EXPORTS = {
     "qgpu_measure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p,
                                C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_uint64)]),
     "qgpu_measure_uniforms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "qgpu_measure_uniforms_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "qgpu_norm": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "qgpu_checksum": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "qgpu_expectation_zzx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),

@@ -16,6 +16,8 @@
 // All sums are f64.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "internal.cuh"
@@ -350,3 +352,107 @@ int qgpu_measure(qgpu_handle* h, uint64_t shots, uint64_t seed, uint64_t* idx_ou
 }
 
 }  // extern "C"
+
+// =============================================================================================
+// Allocation-free sampler: qgpu_measure_uniforms_noalloc
+//
+// Some callers cannot let this library allocate device memory: a host framework that already
+// owns all of the GPU's memory through its own caching pool, or a latency-critical loop that
+// must not enter the CUDA allocator. For them the uniform sampler has a variant whose scratch
+// (chunk sums, chunk offsets, scan workspace, uniform and index staging) lives in the
+// file-scope array below instead of the handle's cudaMalloc'ed buffers. The array is part of
+// this library's device image: every GPU that loads the library holds its
+// NOALLOC_SCRATCH_BYTES until the process exits.
+// =============================================================================================
+namespace qgpu {
+
+constexpr int NOALLOC_MAX_QUBITS = 24;            // register size served (2^15 chunks)
+constexpr uint64_t NOALLOC_MAX_UNIFORMS = 65536;  // uniforms per call
+constexpr uint64_t NOALLOC_MAX_CHUNKS = 1ull << (NOALLOC_MAX_QUBITS - CHUNK_BITS);
+constexpr size_t NOALLOC_SCAN_DOUBLES = 64;       // >= scan_tmp_len(NOALLOC_MAX_CHUNKS)
+constexpr size_t NOALLOC_SCRATCH_BYTES =
+    (2 * NOALLOC_MAX_CHUNKS + 2 + NOALLOC_SCAN_DOUBLES) * sizeof(double) +
+    NOALLOC_MAX_UNIFORMS * (sizeof(double) + sizeof(int64_t));
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch per device. In host code the array's name is only a
+// host-side stand-in, so the address is looked up once per device with that device current.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(int device, unsigned char** out) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return fail(QGPU_ERR_UNSUPPORTED, "qgpu_measure_uniforms_noalloc: device index " +
+                                              std::to_string(device) + " out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        int cur = 0;
+        QGPU_CUDA(cudaGetDevice(&cur));
+        if (cur != device) QGPU_CUDA(cudaSetDevice(device));
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (cur != device) cudaSetDevice(cur);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[device] = p;
+    }
+    *out = (unsigned char*)g_noalloc_ptr[device];
+    return QGPU_OK;
+}
+
+}  // namespace qgpu
+
+extern "C" int qgpu_measure_uniforms_noalloc(qgpu_handle* h, const double* u, size_t n,
+                                             int64_t* out) {
+    if (!h || (n && (!u || !out)))
+        return fail(QGPU_ERR_INVALID, "qgpu_measure_uniforms_noalloc: NULL argument");
+    if (h->n_qubits > NOALLOC_MAX_QUBITS)
+        return fail(QGPU_ERR_INVALID, "qgpu_measure_uniforms_noalloc: the register has " +
+                                          std::to_string(h->n_qubits) + " qubits; at most " +
+                                          std::to_string(NOALLOC_MAX_QUBITS) + " are supported");
+    if (n > NOALLOC_MAX_UNIFORMS)
+        return fail(QGPU_ERR_INVALID, "qgpu_measure_uniforms_noalloc: " + std::to_string(n) +
+                                          " uniforms requested; at most " +
+                                          std::to_string(NOALLOC_MAX_UNIFORMS) + " per call");
+    if (n == 0) return QGPU_OK;
+    unsigned char* base = nullptr;
+    int st = noalloc_scratch(h->device, &base);
+    if (st != QGPU_OK) return st;
+    // Layout of the shared array. Every word this call reads is written earlier in the same
+    // call (sums, offsets, scan tiles, staged uniforms), so nothing needs clearing between calls.
+    Cdf c;
+    const int cb = h->n_qubits < CHUNK_BITS ? h->n_qubits : CHUNK_BITS;
+    c.chunk_len = 1 << cb;
+    c.nchunks = h->dim >> cb;
+    if (scan_tmp_len(c.nchunks) > NOALLOC_SCAN_DOUBLES)
+        return fail(QGPU_ERR_INVALID, "qgpu_measure_uniforms_noalloc: scan workspace too small");
+    double* w = (double*)base;
+    c.sums = w;
+    c.offs = w + NOALLOC_MAX_CHUNKS;
+    c.total = w + 2 * NOALLOC_MAX_CHUNKS;
+    double* scan_tmp = c.total + 2;
+    double* du = scan_tmp + NOALLOC_SCAN_DOUBLES;
+    int64_t* dout = (int64_t*)(du + NOALLOC_MAX_UNIFORMS);
+    const int threads = 256;
+    uint64_t blocks = (c.nchunks * 32 + threads - 1) / threads;
+    if (blocks > (uint64_t)h->sm_count * 16) blocks = (uint64_t)h->sm_count * 16;
+    if (h->precision == QGPU_C128)
+        k_chunk_sums<double2><<<(unsigned)blocks, threads, 0, h->stream>>>(
+            (const double2*)h->state, c.nchunks, c.chunk_len, c.sums);
+    else
+        k_chunk_sums<float2><<<(unsigned)blocks, threads, 0, h->stream>>>(
+            (const float2*)h->state, c.nchunks, c.chunk_len, c.sums);
+    QGPU_CHECK_LAUNCH("k_chunk_sums");
+    h->launches++;
+    QGPU_CUDA(cudaMemcpyAsync(c.offs, c.sums, c.nchunks * sizeof(double), cudaMemcpyDeviceToDevice,
+                              h->stream));
+    st = scan_exclusive(h, c.offs, c.nchunks, scan_tmp, c.total);
+    if (st != QGPU_OK) return st;
+    QGPU_CUDA(copy_async(h, du, u, n * sizeof(double), cudaMemcpyHostToDevice));
+    st = run_sample(h, c, du, n, dout);
+    if (st != QGPU_OK) return st;
+    QGPU_CUDA(copy_async(h, out, dout, n * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    return QGPU_OK;
+}
