@@ -152,6 +152,36 @@ def cpu_reference_sample(n: int, budget_s: float, seed: int = 2) -> dict:
             "seconds": dt, "gates": gates}
 
 
+def adjoint_leg(reps: int = 5) -> dict:
+    """Differentiation config: 20-qubit ansatz, 10 layers of Ry Rz + CNot ring (400 angles),
+    H = sum a_i Z_i Z_i+1 + sum b_i X_i. Adjoint gradient vs parameter shift (+-pi/2, 800 plain
+    simulations + energies) on the same GPU; host wall clock around the blocking calls."""
+    from quantr_gb300 import _native as nat
+    from quantr_gb300 import gradients as GR
+    from quantr_gb300 import workloads as W
+
+    an = W.ansatz(n=20, layers=10, seed=4)
+    prog = an.program()
+    h = nat.Handle(20)
+    e, g = GR.energy_and_gradient(h, prog, an.a, an.b)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        e, g = GR.energy_and_gradient(h, prog, an.a, an.b)
+    t_adj = (time.perf_counter() - t0) / reps
+    GR.energy(h, prog, an.a, an.b)
+    t0 = time.perf_counter()
+    ps = GR.parameter_shift(h, prog, an.a, an.b)
+    t_ps = time.perf_counter() - t0
+    h.close()
+    nparam = int(np.isin(prog.ops["kind"], list(GR.ROTATIONS)).sum())
+    return {"workload": "20q ansatz, 10 layers Ry Rz + CNot ring, ZZ+X observable, c128",
+            "params": nparam, "energy": e, "adjoint_ms": 1e3 * t_adj,
+            "grads_per_s": nparam / t_adj, "param_shift_ms": 1e3 * t_ps,
+            "speedup_vs_param_shift": t_ps / t_adj,
+            "max_abs_diff_vs_param_shift": float(np.max(np.abs(g - ps))),
+            "timer": "host wall clock around blocking calls"}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -304,6 +334,7 @@ def run_ours(args) -> None:
     if world == 1 and not args.no_cpu_baseline:
         cpu = cpu_reference_sample(args.ref_n, budget_s=args.ref_budget)
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    adjoint = None if (args.no_adjoint or world > 1) else adjoint_leg()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -318,7 +349,7 @@ def run_ours(args) -> None:
         "pct_peak": (pass_bytes / (ms_max / 1e3) / 1e9) / peaks["hbm_gbs"],
         "gates_per_s": len(prog.ops) / (ms_max / 1e3),
         "roofline": roofline, "kernels": kernels,
-        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "adjoint": adjoint,
         "clocks": clocks.summary(),
         "result": {"norm": norm, "checksum": [checksum.real, checksum.imag]},
     }
@@ -339,6 +370,7 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--ref-n", type=int, default=14)
     ap.add_argument("--ref-budget", type=float, default=15.0)
     args = ap.parse_args()

@@ -1,0 +1,474 @@
+// quantr.hpp — header-only C++ mirror of quantr's public API (crate 0.6.0, src/lib.rs:78-84) over
+// the C ABI of libquantr_gpu (qgpu.h). Simulation runs on the GPU; there is no CPU fallback.
+//
+//   quantr::Circuit qc = quantr::Circuit::new_(3);
+//   qc.add_gate(quantr::Gate::H(), 2).add_gate(quantr::Gate::CNot(2), 1);
+//   quantr::SimulatedCircuit sim = std::move(qc).simulate();
+//   auto amps = sim.get_state().take().get_amplitudes();
+//   auto bins = sim.measure_all(500).take();           // std::map<ProductState, size_t>
+//
+// Names, argument meaning and error messages follow the Rust crate; Rust's `Result::Err` becomes
+// a thrown quantr::QuantrError. Link with -lquantr_gpu.
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <functional>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <optional>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "qgpu.h"
+
+namespace quantr {
+
+using Complex64 = std::complex<double>;
+
+// src/error.rs:17-33
+struct QuantrError : std::runtime_error {
+    std::string message;
+    explicit QuantrError(const std::string& m)
+        : std::runtime_error("\x1b[91m[Quantr Error] " + m + "\x1b[0m "), message(m) {}
+};
+
+inline void check(int status) {
+    if (status != QGPU_OK) throw QuantrError(qgpu_last_error());
+}
+
+// ---- states (src/circuit/states/) -----------------------------------------------------------
+enum class Qubit : uint8_t { Zero = 0, One = 1 };
+
+class ProductState {
+   public:
+    std::vector<Qubit> qubits;
+
+    ProductState() = default;
+    explicit ProductState(std::vector<Qubit> q) : qubits(std::move(q)) {}
+    static ProductState new_(const std::vector<Qubit>& q) {  // product_states.rs:37-48
+        if (q.empty())
+            throw QuantrError("The slice of qubits is empty, it needs to at least have one element.");
+        return ProductState(q);
+    }
+    static ProductState binary_basis(uint64_t index, size_t n) {  // product_states.rs:205-215
+        std::vector<Qubit> q(n);
+        for (size_t w = 0; w < n; ++w) q[w] = ((index >> (n - 1 - w)) & 1u) ? Qubit::One : Qubit::Zero;
+        return ProductState(q);
+    }
+    uint64_t comp_basis() const {  // product_states.rs:191-201 (64-bit)
+        uint64_t v = 0;
+        for (Qubit q : qubits) v = (v << 1) | (uint64_t)q;
+        return v;
+    }
+    const Qubit* get(size_t i) const { return i < qubits.size() ? &qubits[i] : nullptr; }
+    const std::vector<Qubit>& get_qubits() const { return qubits; }
+    std::vector<Qubit>& get_mut_qubits() { return qubits; }
+    size_t num_qubits() const { return qubits.size(); }
+    ProductState& invert_digit(size_t place) {
+        if (place >= qubits.size())
+            throw QuantrError("The position of the binary digit, " + std::to_string(place) +
+                              ", is out of bounds. The product dimension is " +
+                              std::to_string(qubits.size()) +
+                              ", and so the position must be strictly less.");
+        qubits[place] = qubits[place] == Qubit::Zero ? Qubit::One : Qubit::Zero;
+        return *this;
+    }
+    ProductState kronecker_prod(Qubit q) const {
+        ProductState p = *this;
+        p.qubits.push_back(q);
+        return p;
+    }
+    std::string to_string() const {
+        std::string s;
+        for (Qubit q : qubits) s += q == Qubit::One ? '1' : '0';
+        return s;
+    }
+    bool operator==(const ProductState& o) const { return qubits == o.qubits; }
+    bool operator<(const ProductState& o) const { return qubits < o.qubits; }
+};
+
+class SuperPosition {
+   public:
+    std::vector<Complex64> amplitudes;
+    size_t product_dim = 0;
+
+    SuperPosition() = default;
+    SuperPosition(std::vector<Complex64> a, size_t n) : amplitudes(std::move(a)), product_dim(n) {}
+    static SuperPosition new_(size_t n) {
+        if (n == 0) throw QuantrError("The number of qubits must be non-zero.");
+        std::vector<Complex64> a((size_t)1 << n);
+        a[0] = 1.0;
+        return SuperPosition(std::move(a), n);
+    }
+    static SuperPosition new_with_amplitudes(const std::vector<Complex64>& a) {
+        double t = 0;
+        for (auto& x : a) t += std::norm(x);
+        if (!(t > 1 - 1e-6 && t < 1 + 1e-6))
+            throw QuantrError("Slice given to set amplitudes in super position does not conserve "
+                              "probability, the absolute square sum of the coefficents must be one.");
+        const size_t len = a.size();
+        if (len == 0 || (len & (len - 1)))
+            throw QuantrError("The length of the array must be of the form 2**n where n is an integer.");
+        size_t n = 0;
+        while (((size_t)1 << n) < len) ++n;
+        return SuperPosition(a, n);
+    }
+    static SuperPosition new_with_amplitudes_unchecked(const std::vector<Complex64>& a) {
+        size_t n = 0;
+        while (((size_t)1 << n) < a.size()) ++n;
+        return SuperPosition(a, n);
+    }
+    static SuperPosition from(const ProductState& p) {
+        std::vector<Complex64> a((size_t)1 << p.num_qubits());
+        a[p.comp_basis()] = 1.0;
+        return SuperPosition(std::move(a), p.num_qubits());
+    }
+    std::optional<Complex64> get_amplitude(size_t i) const {
+        if (i < amplitudes.size()) return amplitudes[i];
+        return std::nullopt;
+    }
+    size_t get_num_qubits() const { return product_dim; }
+    size_t get_dimension() const { return amplitudes.size(); }
+    const std::vector<Complex64>& get_amplitudes() const { return amplitudes; }
+    Complex64 get_amplitude_from_state(const ProductState& p) const {
+        if (((size_t)1 << p.num_qubits()) != amplitudes.size())
+            throw QuantrError("Unable to retreive product state, |" + p.to_string() +
+                              "> with dimension " + std::to_string(p.num_qubits()) +
+                              ". The superposition is a linear combination of states with "
+                              "different dimension. These dimensions should be equal.");
+        return amplitudes[p.comp_basis()];
+    }
+    std::map<ProductState, Complex64> to_hash_map() const {  // super_positions.rs:315-323
+        std::map<ProductState, Complex64> m;
+        for (size_t i = 0; i < amplitudes.size(); ++i)
+            if (!(std::norm(amplitudes[i]) < 1e-6 && std::norm(amplitudes[i]) > -1e-6))
+                m[ProductState::binary_basis(i, product_dim)] = amplitudes[i];
+        return m;
+    }
+};
+
+// ---- gates (src/circuit/gate.rs:19-106) --------------------------------------------------------
+using CustomFn = std::function<std::optional<SuperPosition>(const ProductState&)>;
+
+struct Gate {
+    int kind = QGPU_GATE_ID;
+    double angle = 0.0;
+    int k = 0;
+    std::vector<size_t> controls;
+    CustomFn func;
+    std::string name;
+    const void* func_id = nullptr;  // identity of the Custom function for equality
+
+    static Gate make(int kind, std::vector<size_t> c = {}, double a = 0.0, int k = 0) {
+        Gate g;
+        g.kind = kind;
+        g.controls = std::move(c);
+        g.angle = a;
+        g.k = k;
+        return g;
+    }
+    static Gate Id() { return make(QGPU_GATE_ID); }
+    static Gate H() { return make(QGPU_GATE_H); }
+    static Gate X() { return make(QGPU_GATE_X); }
+    static Gate Y() { return make(QGPU_GATE_Y); }
+    static Gate Z() { return make(QGPU_GATE_Z); }
+    static Gate S() { return make(QGPU_GATE_S); }
+    static Gate Sdag() { return make(QGPU_GATE_SDAG); }
+    static Gate T() { return make(QGPU_GATE_T); }
+    static Gate Tdag() { return make(QGPU_GATE_TDAG); }
+    static Gate X90() { return make(QGPU_GATE_X90); }
+    static Gate Y90() { return make(QGPU_GATE_Y90); }
+    static Gate MX90() { return make(QGPU_GATE_MX90); }
+    static Gate MY90() { return make(QGPU_GATE_MY90); }
+    static Gate Rx(double a) { return make(QGPU_GATE_RX, {}, a); }
+    static Gate Ry(double a) { return make(QGPU_GATE_RY, {}, a); }
+    static Gate Rz(double a) { return make(QGPU_GATE_RZ, {}, a); }
+    static Gate Phase(double a) { return make(QGPU_GATE_PHASE, {}, a); }
+    static Gate CR(double a, size_t c) { return make(QGPU_GATE_CR, {c}, a); }
+    static Gate CRk(int kk, size_t c) { return make(QGPU_GATE_CRK, {c}, 0.0, kk); }
+    static Gate CZ(size_t c) { return make(QGPU_GATE_CZ, {c}); }
+    static Gate CY(size_t c) { return make(QGPU_GATE_CY, {c}); }
+    static Gate CNot(size_t c) { return make(QGPU_GATE_CNOT, {c}); }
+    static Gate Swap(size_t c) { return make(QGPU_GATE_SWAP, {c}); }
+    static Gate Toffoli(size_t c1, size_t c2) { return make(QGPU_GATE_TOFFOLI, {c1, c2}); }
+    static Gate Custom(std::optional<SuperPosition> (*f)(const ProductState&),
+                       std::vector<size_t> c, std::string nm) {
+        Gate g = make(QGPU_GATE_CUSTOM, std::move(c));
+        g.func = f;
+        g.func_id = (const void*)f;
+        g.name = std::move(nm);
+        return g;
+    }
+    bool is_single_gate() const { return kind >= QGPU_GATE_ID && kind <= QGPU_GATE_PHASE; }
+    bool is_custom_gate() const { return kind == QGPU_GATE_CUSTOM; }
+    std::optional<std::vector<size_t>> get_nodes() const {
+        if (is_single_gate()) return std::nullopt;
+        return controls;
+    }
+    bool operator==(const Gate& o) const {
+        return kind == o.kind && angle == o.angle && k == o.k && controls == o.controls &&
+               func_id == o.func_id && name == o.name;
+    }
+    bool operator!=(const Gate& o) const { return !(*this == o); }
+};
+
+template <class T>
+struct Measurement {  // src/circuit/measurement.rs:16-27
+    bool observable;
+    T value;
+    T take() { return std::move(value); }
+};
+
+// ---- simulation result (src/simulated_circuit.rs) ----------------------------------------------
+struct HandleDeleter {
+    void operator()(qgpu_handle* h) const { qgpu_destroy(h); }
+};
+using Handle = std::unique_ptr<qgpu_handle, HandleDeleter>;
+
+inline uint64_t& shot_seed() {
+    static uint64_t s = 0;
+    return s;
+}
+// `fastrand::seed` counterpart: reseeds the stream that keys each measure_all call.
+inline void seed(uint64_t s) { shot_seed() = s; }
+
+class SimulatedCircuit {
+   public:
+    SimulatedCircuit(std::vector<Gate> g, size_t n, Handle h, bool progress)
+        : circuit_gates_(std::move(g)), num_qubits_(n), handle_(std::move(h)), progress_(progress) {}
+
+    Measurement<std::map<ProductState, size_t>> measure_all(size_t shots) const {
+        if (!disable_warnings_)
+            for (const Gate& g : circuit_gates_)
+                if (g.is_custom_gate()) {
+                    std::cerr << "\x1b[93m[Quantr Warning] Custom gates were detected in the "
+                                 "circuit. Measurements will be taken from a cached register in "
+                                 "memory, and so if the Custom gate does NOT implement a unitary "
+                                 "mapping, the measure_all method will most likely lead to wrong "
+                                 "results. To simulate a circuit without cache, see "
+                                 "SimulatedCircuit::measure_all_without_cache.\x1b[0m\n";
+                    break;
+                }
+        const size_t cap = std::min<size_t>(shots, (size_t)1 << std::min<size_t>(num_qubits_, 40));
+        std::vector<uint64_t> idx(cap ? cap : 1), cnt(cap ? cap : 1);
+        size_t nu = 0;
+        uint64_t failed = 0;
+        shot_seed() = shot_seed() * 6364136223846793005ull + 1442695040888963407ull;
+        check(qgpu_measure(handle_.get(), shots, shot_seed(), idx.data(), cnt.data(), cap, &nu,
+                           &failed));
+        std::map<ProductState, size_t> bins;
+        for (size_t i = 0; i < nu; ++i)
+            bins[ProductState::binary_basis(idx[i], num_qubits_)] = (size_t)cnt[i];
+        if (failed && !disable_warnings_)
+            std::cerr << "\x1b[93m[Quantr Warning] The superposition failed to collapse to a "
+                         "state during repeat measurements. This is likely due to the use of "
+                         "Gate::Custom where the mapping is not unitary.\x1b[0m\n";
+        return {true, std::move(bins)};
+    }
+    Measurement<SuperPosition> get_state() const {
+        std::vector<Complex64> a((size_t)1 << num_qubits_);
+        check(qgpu_download(handle_.get(), reinterpret_cast<double*>(a.data()), a.size()));
+        return {false, SuperPosition(std::move(a), num_qubits_)};
+    }
+    Measurement<SuperPosition> take_state() const { return get_state(); }
+    void print_warnings(bool printing) { disable_warnings_ = printing; }
+    const std::vector<Gate>& get_circuit_gates() const { return circuit_gates_; }
+    size_t get_num_qubits() const { return num_qubits_; }
+    void set_print_progress(bool p) { progress_ = p; }
+    qgpu_handle* handle() const { return handle_.get(); }
+
+   private:
+    std::vector<Gate> circuit_gates_;
+    size_t num_qubits_;
+    Handle handle_;
+    bool progress_;
+    bool disable_warnings_ = false;
+};
+
+// ---- circuit (src/circuit.rs) -------------------------------------------------------------------
+class Circuit {
+   public:
+    static Circuit new_(size_t n) {  // circuit.rs:48-62
+        if (n == 0) throw QuantrError("The initialised circuit must have at least one wire.");
+        Circuit c;
+        c.num_qubits_ = n;
+        return c;
+    }
+    size_t get_num_qubits() const { return num_qubits_; }
+    void set_print_progress(bool p) { progress_ = p; }
+    const std::vector<Gate>& get_gates() const { return gates_; }
+    // Engine options (not in quantr): QGPU_C128/QGPU_C64 and QGPU_MODE_*.
+    Circuit& set_backend(int precision, int mode) {
+        precision_ = precision;
+        mode_ = mode;
+        return *this;
+    }
+
+    Circuit& add_gate(const Gate& g, size_t position) { return add_gates_with_positions({{position, g}}); }
+
+    Circuit& add_gates_with_positions(const std::map<size_t, Gate>& gp) {  // circuit.rs:152-188
+        for (auto& kv : gp)
+            if (kv.first >= num_qubits_)
+                throw QuantrError("The position, " + std::to_string(kv.first) +
+                                  ", is out of bounds for the circuit with " +
+                                  std::to_string(num_qubits_) + " qubits.");
+        std::vector<Gate> col(num_qubits_, Gate::Id());
+        for (auto& kv : gp) col[kv.first] = kv.second;
+        overlapping(col);
+        push_multi_gates(col);
+        gates_.insert(gates_.end(), col.begin(), col.end());
+        return *this;
+    }
+
+    Circuit& add_gates(const std::vector<Gate>& gates) {  // circuit.rs:210-226
+        if (gates.size() != num_qubits_)
+            throw QuantrError("The number of gates, " + std::to_string(gates.size()) +
+                              ", does not match the number of wires, " +
+                              std::to_string(num_qubits_) + ". All wires must have gates added.");
+        std::vector<Gate> col = gates;
+        overlapping(col);
+        push_multi_gates(col);
+        gates_.insert(gates_.end(), col.begin(), col.end());
+        return *this;
+    }
+
+    Circuit& add_repeating_gate(const Gate& g, const std::vector<size_t>& pos) {
+        std::vector<bool> seen(num_qubits_, false);
+        for (size_t p : pos) {
+            if (p >= num_qubits_ || seen[p])
+                throw QuantrError("Attempted to add more than one gate onto a single wire.");
+            seen[p] = true;
+        }
+        std::vector<Gate> col(num_qubits_, Gate::Id());
+        for (size_t p : pos) col[p] = g;
+        return add_gates(col);
+    }
+
+    Circuit& change_register(const SuperPosition& s) {  // circuit.rs:463-473
+        if (s.product_dim != num_qubits_)
+            throw QuantrError("The custom register has a product state dimension of " +
+                              std::to_string(s.product_dim) + ", while the number of qubits is " +
+                              std::to_string(num_qubits_) + ". These must equal each other.");
+        register_ = s;
+        return *this;
+    }
+
+    SimulatedCircuit simulate() && {  // circuit.rs:364-388
+        auto reg = std::move(register_);
+        register_.reset();
+        return run(reg);
+    }
+    SimulatedCircuit clone_and_simulate() const { return run(register_); }
+
+   private:
+    std::vector<Gate> gates_;
+    size_t num_qubits_ = 0;
+    std::optional<SuperPosition> register_;
+    bool progress_ = false;
+    int precision_ = QGPU_C128;
+    int mode_ = QGPU_MODE_FAST;
+
+    static void push_multi_gates(std::vector<Gate>& gates) {  // circuit.rs:230-270
+        bool found_multi = false, found_second = false;
+        for (const Gate& g : gates) {
+            if (g.is_custom_gate())
+                for (unsigned char ch : g.name)
+                    if (ch > 127)
+                        throw QuantrError("The custom function name, " + g.name +
+                                          ", does not only use ASCII chars.");
+            if (g != Gate::Id()) {
+                if (found_multi) {
+                    found_second = true;
+                    break;
+                }
+                found_multi = true;
+            }
+        }
+        if (!found_second) return;
+        std::vector<Gate> extended;
+        for (size_t pos = 0; pos < gates.size(); ++pos)
+            if (!gates[pos].is_single_gate()) {
+                std::vector<Gate> col(gates.size(), Gate::Id());
+                col[pos] = gates[pos];
+                extended.insert(extended.end(), col.begin(), col.end());
+                gates[pos] = Gate::Id();
+            }
+        gates.insert(gates.end(), extended.begin(), extended.end());
+    }
+
+    void overlapping(const std::vector<Gate>& gates) const {  // circuit.rs:272-293
+        for (size_t pos = 0; pos < gates.size(); ++pos) {
+            auto nodes = gates[pos].get_nodes();
+            if (!nodes) continue;
+            std::vector<bool> seen(num_qubits_, false);
+            for (size_t nd : *nodes) {
+                if (nd >= num_qubits_)
+                    throw QuantrError("The control node at position " + std::to_string(nd) +
+                                      ", is greater than the umnber of qubits " +
+                                      std::to_string(num_qubits_) + ".");
+                if (seen[nd]) throw QuantrError("The gate has overlapping control nodes.");
+                seen[nd] = true;
+                if (nd == pos)
+                    throw QuantrError("The gate has a control node that equals the gate's position " +
+                                      std::to_string(pos) + ".");
+            }
+        }
+    }
+
+    SimulatedCircuit run(const std::optional<SuperPosition>& reg) const {
+        qgpu_handle* raw = nullptr;
+        check(qgpu_create((int)num_qubits_, precision_, &raw));
+        Handle h(raw);
+        check(qgpu_set_mode(h.get(), mode_));
+        if (reg)
+            check(qgpu_upload(h.get(), reinterpret_cast<const double*>(reg->amplitudes.data()),
+                              reg->amplitudes.size()));
+        // lowering: simulation.rs:37-56
+        std::vector<qgpu_op> ops;
+        std::vector<double> mats;
+        std::vector<uint8_t> none;
+        size_t counter = 0;
+        for (const Gate& g : gates_) {
+            if (g.kind == QGPU_GATE_ID) {
+                ++counter;
+                continue;
+            }
+            qgpu_op op{};
+            op.kind = g.kind;
+            op.target = (int32_t)(counter % num_qubits_);
+            op.n_controls = (int32_t)g.controls.size();
+            for (size_t m = 0; m < g.controls.size() && m < QGPU_MAX_OP_WIRES; ++m)
+                op.controls[m] = (int32_t)g.controls[m];
+            op.param = g.angle;
+            op.k = g.k;
+            if (g.is_custom_gate()) {  // simulation.rs:137-156, tabulated
+                const size_t kq = g.controls.size() + 1, d = (size_t)1 << kq;
+                op.mat_offset = (int64_t)mats.size();
+                op.none_offset = (int64_t)none.size();
+                for (size_t j = 0; j < d; ++j) {
+                    auto img = g.func(ProductState::binary_basis(j, kq));
+                    none.push_back(img ? 0 : 1);
+                    for (size_t l = 0; l < d; ++l) {
+                        Complex64 v = (img && l < img->amplitudes.size()) ? img->amplitudes[l] : 0.0;
+                        mats.push_back(v.real());
+                        mats.push_back(v.imag());
+                    }
+                }
+            }
+            if (progress_)
+                std::cout << "Applying gate " << g.kind << " on wire " << op.target << " # "
+                          << counter + 1 << "/" << gates_.size() << " \n";
+            ops.push_back(op);
+            ++counter;
+        }
+        check(qgpu_apply_program(h.get(), ops.data(), ops.size(), mats.data(), mats.size(),
+                                 none.data(), none.size()));
+        return SimulatedCircuit(gates_, num_qubits_, std::move(h), progress_);
+    }
+};
+
+}  // namespace quantr

@@ -53,6 +53,7 @@ struct qgpu_handle {
     void* active = nullptr;    // when set, gate passes run on this buffer instead of `state`
     cudaStream_t stream = nullptr;
     qgpu::Scratch gates;       // per-program device tables (custom matrices, orders, flags)
+    qgpu::Scratch tables;      // per-program phase tables of fused diagonal runs
     qgpu::Scratch work;        // reductions, measurement buffers
     qgpu::Scratch work2;       // second buffer (measurement indices / adjoint vectors)
     uint64_t launches = 0;     // kernels launched on this handle (for benchmarking claims)
@@ -112,26 +113,21 @@ struct ffc {  // complex value with float-pair real and imaginary parts
 
 // f64 -> float pair by bit manipulation (the f64<->f32 conversion instructions run on the slow
 // FP64 pipe). h takes the sign, exponent and top 23 fraction bits (truncated). The remaining 29
-// fraction bits are rebuilt as two exact floats with the 2^23 "magic number" subtraction (23
-// bits, then 6 bits) whose sum rounds to nearest, so |x - (h + l)| <= 2^-48 |x| without bias.
-// Values below 2^-126 in magnitude become 0; the low part is dropped below 2^-97.
+// fraction bits become l, rounded to nearest, so |x - (h + l)| <= 2^-48 |x| without bias.
+// Values below 2^-126 in magnitude become 0; the low part is dropped below 2^-75.
 __device__ __forceinline__ void split_f64(double x, float& h, float& l) {
     const unsigned lo = (unsigned)__double2loint(x);
     const unsigned hi = (unsigned)__double2hiint(x);
-    const unsigned ex = (hi >> 20) & 0x7FFu;
     const unsigned t = hi - (896u << 20);            // rebias 1023 -> 127 (valid when ex > 896)
     unsigned hb = __funnelshift_l(lo, t, 3);          // (t << 3) | (lo >> 29)
     hb = (hb & 0x7FFFFFFFu) | (hi & 0x80000000u);
-    const unsigned ea = (hb & 0x7F800000u) - (23u << 23);  // 2^23 * 2^(E-1069): weight of bit 6
-    const unsigned eb = ea - (6u << 23);                   // 2^23 * 2^(E-1075): weight of bit 0
-    const float ra = __fsub_rn(__uint_as_float(ea | ((lo >> 6) & 0x7FFFFFu)), __uint_as_float(ea));
-    const float rb = __fsub_rn(__uint_as_float(eb | (lo & 0x3Fu)), __uint_as_float(eb));
-    float lf = __fadd_rn(ra, rb);
-    lf = __uint_as_float(__float_as_uint(lf) | (hi & 0x80000000u));
-    const bool tiny = ex <= 896u;
-    const bool nolo = ex <= 925u;
-    h = tiny ? 0.0f : __uint_as_float(hb);
-    l = nolo ? 0.0f : lf;
+    // remaining 29 fraction bits: an integer m29 with weight 2^(E-1075); the integer->float
+    // conversion rounds it to nearest, the power-of-two scale (carrying x's sign) is exact
+    const float m = __uint2float_rn(lo & 0x1FFFFFFFu);
+    const float scale = __uint_as_float((hb & 0xFF800000u) - (52u << 23));
+    const unsigned ah = hi & 0x7FFFFFFFu;
+    h = ah <= (896u << 20) + 0xFFFFFu ? 0.0f : __uint_as_float(hb);  // |x| < 2^-126 -> 0
+    l = ah <= (948u << 20) + 0xFFFFFu ? 0.0f : __fmul_rn(m, scale);  // drop below 2^-75
 }
 
 // Exact float -> f64 by bit manipulation (zero and subnormal floats give a signed zero).
@@ -145,9 +141,19 @@ __device__ __forceinline__ double f32_to_f64_bits(float f) {
     return __hiloint2double((int)hiw, (int)low);
 }
 
-// float pair -> f64: both halves are exact doubles; one f64 add rounds their sum.
+// Exact float -> f64 for normal floats only (a zero or subnormal float maps to a value of
+// magnitude below 2^-126 instead of 0; join_f64 handles the zero high part).
+__device__ __forceinline__ double f32_to_f64_normal(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned hiw = (((b & 0x7FFFFFFFu) >> 3) + (896u << 20)) | (b & 0x80000000u);
+    return __hiloint2double((int)hiw, (int)(b << 29));
+}
+
+// float pair -> f64: both halves are exact doubles; one f64 add rounds their sum. A high part
+// below the float normal range (the pair is then below 2^-126) gives 0.
 __device__ __forceinline__ double join_f64(float h, float l) {
-    return __dadd_rn(f32_to_f64_bits(h), f32_to_f64_bits(l));
+    const double d = __dadd_rn(f32_to_f64_normal(h), f32_to_f64_normal(l));
+    return (__float_as_uint(h) & 0x7F800000u) ? d : 0.0;
 }
 
 __device__ __forceinline__ ffc to_ffc(double2 a) {
@@ -159,6 +165,90 @@ __device__ __forceinline__ ffc to_ffc(double2 a) {
 __device__ __forceinline__ double2 from_ffc(const ffc& a) {
     return make_double2(join_f64(a.rh, a.rl), join_f64(a.ih, a.il));
 }
+
+// ---- packed f32x2 arithmetic (Blackwell add/sub/mul/fma .rn.f32x2) ---------------------------
+// A 64-bit register holds two floats (lane 0, lane 1); each op rounds each lane to nearest,
+// exactly as the scalar instruction would, so the error-free transforms hold lane by lane.
+typedef uint64_t u64;
+
+__device__ __forceinline__ u64 p2(float x, float y) {
+    u64 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+    return r;
+}
+__device__ __forceinline__ void up2(u64 v, float& x, float& y) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+}
+__device__ __forceinline__ u64 pmul(u64 a, u64 b) {
+    u64 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 pfma(u64 a, u64 b, u64 c) {
+    u64 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ u64 padd(u64 a, u64 b) {
+    u64 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 psub(u64 a, u64 b) {
+    u64 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 pswap(u64 v) {
+    float x, y;
+    up2(v, x, y);
+    return p2(y, x);
+}
+
+// Complex value as float pairs, packed by part: h = (re_hi, im_hi), l = (re_lo, im_lo).
+struct ffp {
+    u64 h, l;
+};
+
+__device__ __forceinline__ ffp to_ffp(double2 a) {
+    float rh, rl, ih, il;
+    split_f64(a.x, rh, rl);
+    split_f64(a.y, ih, il);
+    return ffp{p2(rh, ih), p2(rl, il)};
+}
+__device__ __forceinline__ double2 from_ffp(const ffp& v) {
+    float rh, ih, rl, il;
+    up2(v.h, rh, ih);
+    up2(v.l, rl, il);
+    return make_double2(join_f64(rh, rl), join_f64(ih, il));
+}
+
+// Dot2 on both lanes at once. A term's constants are c[0..3] = (U_hi, U_lo, -U_hi, -U_lo);
+// `en` holds the negated error sum so that every update is a single fma/add/sub.
+struct PDot2 {
+    u64 s, en;
+    __device__ __forceinline__ void first(const u64* c, u64 xh, u64 xl) {
+        s = pmul(c[0], xh);
+        en = pfma(c[2], xh, s);   // s - Uh*xh: minus the product's rounding error
+        en = pfma(c[2], xl, en);  // - Uh*xl
+        en = pfma(c[3], xh, en);  // - Ul*xh
+    }
+    __device__ __forceinline__ void add(const u64* c, u64 xh, u64 xl) {
+        const u64 p = pmul(c[0], xh);
+        u64 rn = pfma(c[2], xh, p);
+        rn = pfma(c[2], xl, rn);
+        rn = pfma(c[3], xh, rn);
+        const u64 t = padd(s, p);  // TwoSum(s, p)
+        const u64 bb = psub(t, s);
+        const u64 q = padd(psub(s, psub(t, bb)), psub(p, bb));
+        s = t;
+        en = padd(psub(en, q), rn);
+    }
+    __device__ __forceinline__ void result(u64& h, u64& l) const {  // FastTwoSum(s, -en)
+        h = psub(s, en);
+        l = psub(psub(s, h), en);
+    }
+};
 
 // Accurate dot product accumulator (Ogita, Rump & Oishi 2005, "Dot2"): s carries the running
 // sum of the leading products, e collects every rounding error plus the small cross products.

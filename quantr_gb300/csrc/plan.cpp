@@ -235,6 +235,56 @@ void set_entry(DevStep& s, int slot, cd x) {
     s.d[2 * slot + 1] = x.imag();
 }
 
+uint64_t pack2(float lane0, float lane1) {
+    uint32_t a, b;
+    std::memcpy(&a, &lane0, 4);
+    std::memcpy(&b, &lane1, 4);
+    return (uint64_t)a | ((uint64_t)b << 32);
+}
+
+// One Dot2 term with per-lane coefficients (c0 for the real output lane, c1 for the imaginary).
+void set_term(DevStep& s, int term, double c0, double c1) {
+    const float h0 = (float)c0, h1 = (float)c1;
+    const float l0 = (float)(c0 - (double)h0), l1 = (float)(c1 - (double)h1);
+    s.pk[4 * term + 0] = pack2(h0, h1);
+    s.pk[4 * term + 1] = pack2(l0, l1);
+    s.pk[4 * term + 2] = pack2(-h0, -h1);
+    s.pk[4 * term + 3] = pack2(-l0, -l1);
+}
+
+// Packed terms of "out = c * x" for complex c: (re, im) = (cr, cr) (x.r, x.i) + (-ci, ci) (x.i, x.r)
+void set_scalar_terms(DevStep& s, int first_term, cd c) {
+    set_term(s, first_term, c.real(), c.real());
+    set_term(s, first_term + 1, -c.imag(), c.imag());
+}
+
+// Packed constants of the float-pair kernels for a step whose entries are already set.
+void set_packed(DevStep& s, const cd* e) {
+    switch (s.type) {
+        case ST_DENSE:  // out0 = e0 a + e1 b ; out1 = e2 a + e3 b
+            set_scalar_terms(s, 0, e[0]);
+            set_scalar_terms(s, 2, e[1]);
+            set_scalar_terms(s, 4, e[2]);
+            set_scalar_terms(s, 6, e[3]);
+            break;
+        case ST_REAL:
+            set_term(s, 0, e[0].real(), e[0].real());
+            set_term(s, 1, e[1].real(), e[1].real());
+            set_term(s, 2, e[2].real(), e[2].real());
+            set_term(s, 3, e[3].real(), e[3].real());
+            break;
+        case ST_PHASE:
+            set_scalar_terms(s, 0, e[0]);
+            break;
+        case ST_DIAG:
+            set_scalar_terms(s, 0, e[0]);
+            set_scalar_terms(s, 2, e[1]);
+            break;
+        default:
+            break;
+    }
+}
+
 // Host-side step with its full-index bit(s) still unresolved to tile positions.
 struct HStep {
     DevStep s;
@@ -287,6 +337,7 @@ void emit_one(const AGate& g, std::vector<HStep>& out) {
             h.s = blank_step(ST_PHASE);
             h.s.cm = g.cm | (1ull << g.t);
             set_entry(h.s, 0, u11);
+            set_packed(h.s, &u11);
             h.unit = c1 >= 0;
             h.s.unit = h.unit;
             h.s.u0 = (uint8_t)(c1 < 0 ? 0 : c1);
@@ -298,6 +349,8 @@ void emit_one(const AGate& g, std::vector<HStep>& out) {
             h.s.fb = (uint8_t)g.t;
             set_entry(h.s, 0, u00);
             set_entry(h.s, 1, u11);
+            const cd dd[2] = {u00, u11};
+            set_packed(h.s, dd);
             h.unit = c0 >= 0 && c1 >= 0;
             h.s.unit = h.unit;
             h.s.u0 = (uint8_t)(c0 < 0 ? 0 : c0);
@@ -327,6 +380,8 @@ void emit_one(const AGate& g, std::vector<HStep>& out) {
     set_entry(h.s, 1, u01);
     set_entry(h.s, 2, u10);
     set_entry(h.s, 3, u11);
+    const cd ee[4] = {u00, u01, u10, u11};
+    set_packed(h.s, ee);
     h.need[0] = g.t;
     out.push_back(h);
 }
@@ -609,7 +664,9 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
         const int c = step_cost(h, opt.policy);
         const bool arith = !h.unit;
         const int new_cost = cur_cost + c + ((arith && !cur_arith) ? conv : 0);
-        const bool fits = (int)bits.size() <= max_bits && (int)cur_steps.size() < MAX_STEPS &&
+        const int width = (arith || cur_arith) ? std::min(max_bits, std::max(1, opt.max_arith_bits))
+                                               : max_bits;
+        const bool fits = (int)bits.size() <= width && (int)cur_steps.size() < MAX_STEPS &&
                           (cur_steps.empty() || new_cost <= opt.budget);
         if (!fits) {
             flush();

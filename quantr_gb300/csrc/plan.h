@@ -61,6 +61,11 @@ struct DevStep {
     uint8_t nfields, pad[3];
     float ff[16];                      // up to 4 complex entries as float pairs
     double d[8];                       // the same entries in f64
+    // Packed f32x2 operands of the float-pair kernels: term t of a Dot2 uses
+    // pk[4t..4t+3] = (U_hi, U_lo, -U_hi, -U_lo), each lane pair (for the real, imag output).
+    // DENSE: outputs 0 and 1, terms 0..3 each (slots 0..15, 16..31); REAL: terms 0..1 per
+    // output; PHASE: one complex constant (slots 0..7); DIAG: two (slots 0..7, 8..15).
+    uint64_t pk[32];
 };
 
 struct Pass {
@@ -85,6 +90,7 @@ enum ArithPolicy { POL_FF = 0, POL_F64 = 1, POL_F32 = 2 };
 struct PlanOptions {
     int policy = POL_FF;               // arithmetic the passes will run in (sets step costs)
     int max_bits = MAX_TILE_BITS;      // tile width (register tile of 2^bits amplitudes)
+    int max_arith_bits = MAX_TILE_BITS;  // tile width of passes that carry arithmetic
     int budget = 100;                  // arithmetic ops per amplitude a pass may carry
     bool merge_1q = true;              // multiply runs of single-wire gates into one matrix
     bool fuse_diagonal = true;         // fold diagonal runs into phase tables

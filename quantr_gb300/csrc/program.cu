@@ -218,16 +218,20 @@ template <class R>
 __device__ __forceinline__ void unit_mul(R& a, int code);
 
 template <>
-__device__ __forceinline__ void unit_mul<ffc>(ffc& a, int code) {
-    if (code == 1) {
-        ffc r{-a.ih, -a.il, a.rh, a.rl};
-        a = r;
+__device__ __forceinline__ void unit_mul<ffp>(ffp& a, int code) {
+    if (code == 0) return;
+    float rh, ih, rl, il;
+    up2(a.h, rh, ih);
+    up2(a.l, rl, il);
+    if (code == 1) {  // (re, im) -> (-im, re)
+        a.h = p2(-ih, rh);
+        a.l = p2(-il, rl);
     } else if (code == 2) {
-        ffc r{-a.rh, -a.rl, -a.ih, -a.il};
-        a = r;
-    } else if (code == 3) {
-        ffc r{a.ih, a.il, -a.rh, -a.rl};
-        a = r;
+        a.h = p2(-rh, -ih);
+        a.l = p2(-rl, -il);
+    } else {  // (re, im) -> (im, -re)
+        a.h = p2(ih, -rh);
+        a.l = p2(il, -rl);
     }
 }
 template <>
@@ -244,73 +248,60 @@ __device__ __forceinline__ void unit_mul<float2>(float2& a, int code) {
 }
 
 // ---- float-pair policy: complex128 storage, f64 arithmetic emulated on FP32/INT pipes -------
+// Each complex value is two packed registers (ffp); one Dot2 computes the real and imaginary
+// output lanes together: out = sum_t (c_t lanes) * (x_t lanes) with x_t = a, swap(a), b, swap(b).
 struct PolFF {
     using S = double2;
-    using R = ffc;
-    static __device__ __forceinline__ R load(S a) { return to_ffc(a); }
-    static __device__ __forceinline__ S store(const R& r) { return from_ffc(r); }
-    // out0 = u00 a + u01 b ; out1 = u10 a + u11 b ; m = 4 float-pair complex entries
-    static __device__ __forceinline__ void dense(R& a, R& b, const float* m) {
-        Dot2 d;
+    using R = ffp;
+    static __device__ __forceinline__ R load(S a) { return to_ffp(a); }
+    static __device__ __forceinline__ S store(const R& r) { return from_ffp(r); }
+    // out0 = u00 a + u01 b ; out1 = u10 a + u11 b (packed terms, DevStep::pk)
+    static __device__ __forceinline__ void dense(R& a, R& b, const DevStep& s) {
+        const u64* c = s.pk;
+        const u64 ash = pswap(a.h), asl = pswap(a.l), bsh = pswap(b.h), bsl = pswap(b.l);
+        PDot2 d;
         R o0, o1;
-        d.first(m[0], m[1], a.rh, a.rl);
-        d.add(-m[2], -m[3], a.ih, a.il);
-        d.add(m[4], m[5], b.rh, b.rl);
-        d.add(-m[6], -m[7], b.ih, b.il);
-        d.result(o0.rh, o0.rl);
-        d.first(m[0], m[1], a.ih, a.il);
-        d.add(m[2], m[3], a.rh, a.rl);
-        d.add(m[4], m[5], b.ih, b.il);
-        d.add(m[6], m[7], b.rh, b.rl);
-        d.result(o0.ih, o0.il);
-        d.first(m[8], m[9], a.rh, a.rl);
-        d.add(-m[10], -m[11], a.ih, a.il);
-        d.add(m[12], m[13], b.rh, b.rl);
-        d.add(-m[14], -m[15], b.ih, b.il);
-        d.result(o1.rh, o1.rl);
-        d.first(m[8], m[9], a.ih, a.il);
-        d.add(m[10], m[11], a.rh, a.rl);
-        d.add(m[12], m[13], b.ih, b.il);
-        d.add(m[14], m[15], b.rh, b.rl);
-        d.result(o1.ih, o1.il);
+        d.first(c + 0, a.h, a.l);
+        d.add(c + 4, ash, asl);
+        d.add(c + 8, b.h, b.l);
+        d.add(c + 12, bsh, bsl);
+        d.result(o0.h, o0.l);
+        d.first(c + 16, a.h, a.l);
+        d.add(c + 20, ash, asl);
+        d.add(c + 24, b.h, b.l);
+        d.add(c + 28, bsh, bsl);
+        d.result(o1.h, o1.l);
         a = o0;
         b = o1;
     }
-    static __device__ __forceinline__ void real(R& a, R& b, const float* m) {
-        Dot2 d;
+    static __device__ __forceinline__ void real(R& a, R& b, const DevStep& s) {
+        const u64* c = s.pk;
+        PDot2 d;
         R o0, o1;
-        d.first(m[0], m[1], a.rh, a.rl);
-        d.add(m[4], m[5], b.rh, b.rl);
-        d.result(o0.rh, o0.rl);
-        d.first(m[0], m[1], a.ih, a.il);
-        d.add(m[4], m[5], b.ih, b.il);
-        d.result(o0.ih, o0.il);
-        d.first(m[8], m[9], a.rh, a.rl);
-        d.add(m[12], m[13], b.rh, b.rl);
-        d.result(o1.rh, o1.rl);
-        d.first(m[8], m[9], a.ih, a.il);
-        d.add(m[12], m[13], b.ih, b.il);
-        d.result(o1.ih, o1.il);
+        d.first(c + 0, a.h, a.l);
+        d.add(c + 4, b.h, b.l);
+        d.result(o0.h, o0.l);
+        d.first(c + 8, a.h, a.l);
+        d.add(c + 12, b.h, b.l);
+        d.result(o1.h, o1.l);
         a = o0;
         b = o1;
     }
-    static __device__ __forceinline__ void mul(R& a, float ch, float cl, float sh_, float sl) {
-        Dot2 d;
-        R o;
-        d.first(ch, cl, a.rh, a.rl);
-        d.add(-sh_, -sl, a.ih, a.il);
-        d.result(o.rh, o.rl);
-        d.first(ch, cl, a.ih, a.il);
-        d.add(sh_, sl, a.rh, a.rl);
-        d.result(o.ih, o.il);
-        a = o;
+    // a *= c, with c's two packed terms at c[0..7]
+    static __device__ __forceinline__ void mul_pk(R& a, const u64* c) {
+        PDot2 d;
+        d.first(c, a.h, a.l);
+        d.add(c + 4, pswap(a.h), pswap(a.l));
+        d.result(a.h, a.l);
     }
     static __device__ __forceinline__ void mul_slot(R& a, const DevStep& s, int slot) {
-        mul(a, s.ff[4 * slot], s.ff[4 * slot + 1], s.ff[4 * slot + 2], s.ff[4 * slot + 3]);
+        mul_pk(a, s.pk + 8 * slot);
     }
     static __device__ __forceinline__ void mul_table(R& a, const TileParams& p, uint32_t e) {
-        const float4 c = __ldg(p.tab_ff + e);
-        mul(a, c.x, c.y, c.z, c.w);
+        const float4 v = __ldg(p.tab_ff + e);  // (re_h, re_l, im_h, im_l)
+        const u64 c[8] = {p2(v.x, v.x), p2(v.y, v.y), p2(-v.x, -v.x), p2(-v.y, -v.y),
+                          p2(-v.z, v.z), p2(-v.w, v.w), p2(v.z, -v.z), p2(v.w, -v.w)};
+        mul_pk(a, c);
     }
 };
 
@@ -323,13 +314,15 @@ struct PolF64 {
     static __device__ __forceinline__ double2 cmla(double2 acc, double ur, double ui, double2 x) {
         return make_double2(fma(ur, x.x, fma(-ui, x.y, acc.x)), fma(ur, x.y, fma(ui, x.x, acc.y)));
     }
-    static __device__ __forceinline__ void dense(R& a, R& b, const double* m) {
+    static __device__ __forceinline__ void dense(R& a, R& b, const DevStep& s) {
+        const double* m = s.d;
         double2 o0 = cmla(cmla(make_double2(0, 0), m[0], m[1], a), m[2], m[3], b);
         double2 o1 = cmla(cmla(make_double2(0, 0), m[4], m[5], a), m[6], m[7], b);
         a = o0;
         b = o1;
     }
-    static __device__ __forceinline__ void real(R& a, R& b, const double* m) {
+    static __device__ __forceinline__ void real(R& a, R& b, const DevStep& s) {
+        const double* m = s.d;
         double2 o0 = make_double2(fma(m[0], a.x, m[2] * b.x), fma(m[0], a.y, m[2] * b.y));
         double2 o1 = make_double2(fma(m[4], a.x, m[6] * b.x), fma(m[4], a.y, m[6] * b.y));
         a = o0;
@@ -356,14 +349,16 @@ struct PolF32 {
     static __device__ __forceinline__ float2 cmla(float2 acc, float ur, float ui, float2 x) {
         return make_float2(fmaf(ur, x.x, fmaf(-ui, x.y, acc.x)), fmaf(ur, x.y, fmaf(ui, x.x, acc.y)));
     }
-    static __device__ __forceinline__ void dense(R& a, R& b, const float* m) {
+    static __device__ __forceinline__ void dense(R& a, R& b, const DevStep& s) {
         // hi parts of the float-pair entries are the entries rounded to f32
+        const float* m = s.ff;
         float2 o0 = cmla(cmla(make_float2(0, 0), m[0], m[2], a), m[4], m[6], b);
         float2 o1 = cmla(cmla(make_float2(0, 0), m[8], m[10], a), m[12], m[14], b);
         a = o0;
         b = o1;
     }
-    static __device__ __forceinline__ void real(R& a, R& b, const float* m) {
+    static __device__ __forceinline__ void real(R& a, R& b, const DevStep& s) {
+        const float* m = s.ff;
         float2 o0 = make_float2(fmaf(m[0], a.x, m[4] * b.x), fmaf(m[0], a.y, m[4] * b.y));
         float2 o1 = make_float2(fmaf(m[8], a.x, m[12] * b.x), fmaf(m[8], a.y, m[12] * b.y));
         a = o0;
@@ -391,21 +386,6 @@ struct PolRaw {
 };
 
 template <class P>
-struct Consts;
-template <>
-struct Consts<PolFF> {
-    static __device__ __forceinline__ const float* m(const DevStep& s) { return s.ff; }
-};
-template <>
-struct Consts<PolF32> {
-    static __device__ __forceinline__ const float* m(const DevStep& s) { return s.ff; }
-};
-template <>
-struct Consts<PolF64> {
-    static __device__ __forceinline__ const double* m(const DevStep& s) { return s.d; }
-};
-
-template <class P>
 struct IsArith { static constexpr bool value = true; };
 template <class T>
 struct IsArith<PolRaw<T>> { static constexpr bool value = false; };
@@ -430,8 +410,8 @@ __device__ __forceinline__ void step_on_bit(typename P::R* v, const DevStep& s, 
             unit_mul(v[j1], s.u1);
         } else {
             if constexpr (IsArith<P>::value) {
-                if (s.type == ST_DENSE) P::dense(v[j], v[j1], Consts<P>::m(s));
-                else P::real(v[j], v[j1], Consts<P>::m(s));
+                if (s.type == ST_DENSE) P::dense(v[j], v[j1], s);
+                else P::real(v[j], v[j1], s);
             }
         }
     }
@@ -539,16 +519,23 @@ __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, co
                 for (int j = 0; j < T; ++j) raw[u][j] = st[b | off[j]];
             }
         }
+        typename P::R v[U][T];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int j = 0; j < T; ++j) v[u][j] = P::load(raw[u][j]);
+        // step-major: each step's constants and dispatch are read once for all U groups
+        for (int s = 0; s < p.nsteps; ++s) {
+            const DevStep& sp = p.steps[s];
+#pragma unroll
+            for (int u = 0; u < U; ++u) step_tile<K, P>(v[u], sp, base[u], off, p);
+        }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint64_t g = g0 + (uint64_t)u * blockDim.x + threadIdx.x;
             if (g >= p.ngroups) continue;
-            typename P::R v[T];
 #pragma unroll
-            for (int j = 0; j < T; ++j) v[j] = P::load(raw[u][j]);
-            for (int s = 0; s < p.nsteps; ++s) step_tile<K, P>(v, p.steps[s], base[u], off, p);
-#pragma unroll
-            for (int j = 0; j < T; ++j) st[base[u] | off[j]] = P::store(v[j]);
+            for (int j = 0; j < T; ++j) st[base[u] | off[j]] = P::store(v[u][j]);
         }
     }
 }
@@ -567,11 +554,18 @@ static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
     return QGPU_OK;
 }
 
+static int env_int(const char* name, int dflt);
+
 template <class P>
 static int launch_tile_k(qgpu_handle* h, const TileParams& p) {
+    // Groups per thread: 4 amplitudes live per thread (8 for 3-bit tiles) keeps the float-pair
+    // passes near 56 registers and 4 CTAs per SM; measured on GB300, 2 groups of a 1-bit tile
+    // ran 17 % faster than 4.
+    static const int k1_groups = env_int("QGPU_K1_GROUPS", 2);  // tuning knob: 2 or 4
     switch (p.nbits) {
-        case 1: return launch_tile_t<1, 4, P>(h, p);
-        case 2: return launch_tile_t<2, 2, P>(h, p);
+        case 1:
+            return k1_groups == 4 ? launch_tile_t<1, 4, P>(h, p) : launch_tile_t<1, 2, P>(h, p);
+        case 2: return launch_tile_t<2, 1, P>(h, p);
         default: return launch_tile_t<3, 1, P>(h, p);
     }
 }
@@ -598,14 +592,14 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
     const double2* tab_f64 = nullptr;
     if (nent) {
         const size_t ffb = align_up(nent * 16, 256);
-        int st = h->work2.ensure(ffb + nent * 16);
+        int st = h->tables.ensure(ffb + nent * 16);
         if (st != QGPU_OK) return st;
-        QGPU_CUDA(copy_async(h, h->work2.ptr, plan.table_ff.data(), nent * 16,
+        QGPU_CUDA(copy_async(h, h->tables.ptr, plan.table_ff.data(), nent * 16,
                              cudaMemcpyHostToDevice));
-        QGPU_CUDA(copy_async(h, (uint8_t*)h->work2.ptr + ffb, plan.table_f64.data(), nent * 16,
+        QGPU_CUDA(copy_async(h, (uint8_t*)h->tables.ptr + ffb, plan.table_f64.data(), nent * 16,
                              cudaMemcpyHostToDevice));
-        tab_ff = (const float4*)h->work2.ptr;
-        tab_f64 = (const double2*)((uint8_t*)h->work2.ptr + ffb);
+        tab_ff = (const float4*)h->tables.ptr;
+        tab_f64 = (const double2*)((uint8_t*)h->tables.ptr + ffb);
     }
     // Custom blocks: upload their tables once
     std::vector<const LocalGate*> blocks;
@@ -695,6 +689,9 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     else if (o.policy == POL_F32) o.budget = env_int("QGPU_F32_BUDGET", 48);
     else o.budget = env_int("QGPU_F64_BUDGET", 1 << 20);
     o.max_bits = std::max(2, std::min(env_int("QGPU_TILE_BITS", MAX_TILE_BITS), MAX_TILE_BITS));
+    // float-pair arithmetic on 8 amplitudes per thread needs ~120 registers (2 CTAs per SM):
+    // keep arithmetic passes at 2 tile bits
+    o.max_arith_bits = o.policy == POL_FF ? env_int("QGPU_ARITH_TILE_BITS", 2) : MAX_TILE_BITS;
     return o;
 }
 

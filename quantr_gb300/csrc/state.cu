@@ -302,6 +302,7 @@ int qgpu_destroy(qgpu_handle* h) {
     if (!h) return QGPU_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     h->gates.release();
+    h->tables.release();
     h->work.release();
     h->work2.release();
     for (cudaEvent_t e : h->events) cudaEventDestroy(e);
