@@ -107,6 +107,11 @@ int qgpu_create(int n_qubits, int precision, qgpu_handle** out);
 int qgpu_destroy(qgpu_handle* h);
 int qgpu_num_qubits(const qgpu_handle* h);
 int qgpu_set_mode(qgpu_handle* h, int mode);             /* QGPU_MODE_*                  */
+/* Dense-block fusion (no counterpart in quantr): when block_qubits is 1..6, qgpu_apply_program
+ * multiplies runs of at most max_gates consecutive gates acting on at most block_qubits wires
+ * into one 2^k x 2^k complex matrix on the host and applies each with one pass. 0 (default)
+ * restores the register-tile passes. QGPU_MODE_EXACT ignores it. */
+int qgpu_set_fusion(qgpu_handle* h, int block_qubits, int max_gates);
 const char* qgpu_last_error(void);                        /* thread-local, never NULL     */
 
 /* ---- register in / out ------------------------------------------------------------------ */
@@ -172,6 +177,25 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
                       const double* mats, size_t n_mat_doubles,
                       const uint8_t* none_flags, size_t n_none_flags,
                       const double* a, const double* b, double* energy, double* grads);
+
+/* ---- batching (no counterpart in quantr) --------------------------------------------------
+ * Many independent circuits, each started from |0...0>, each with its own ZZ+X observable:
+ * energies[i] and d energy / d angle for every op (grads[grad_offset + g]). Circuits small
+ * enough for shared memory (complex128 <= 12 qubits, complex64 <= 13) run in one persistent
+ * launch replayed from a CUDA graph; larger ones run through the register-tile passes with a
+ * per-size fusion budget picked by timing (written to tuned_budget[n_qubits] when not NULL,
+ * an int[41]). Custom gates are rejected (QGPU_ERR_NONUNITARY). */
+typedef struct qgpu_batch_item {
+    int32_t n_qubits;
+    int32_t n_ops;
+    int64_t op_offset;    /* first op in ops[]                                  */
+    int64_t obs_offset;   /* a[n_qubits] then b[n_qubits] start at obs[...]     */
+    int64_t grad_offset;  /* n_ops gradient slots start at grads[...]           */
+} qgpu_batch_item;
+
+int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, const qgpu_op* ops,
+                   size_t n_ops_total, const double* obs, size_t n_obs, int precision,
+                   double* energies, double* grads, int* tuned_budget);
 
 /* ---- engine introspection (no counterpart in quantr) ------------------------------------ */
 

@@ -52,6 +52,7 @@ _EXPORTS = {
     "qgpu_destroy": (C.c_int, [C.c_void_p]),
     "qgpu_num_qubits": (C.c_int, [C.c_void_p]),
     "qgpu_set_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "qgpu_set_fusion": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "qgpu_last_error": (C.c_char_p, []),
     "qgpu_set_zero": (C.c_int, [C.c_void_p]),
     "qgpu_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
@@ -134,6 +135,10 @@ class Handle:
     def set_mode(self, mode: int) -> None:
         check(lib().qgpu_set_mode(self._h, int(mode)), "qgpu_set_mode")
         self.mode = mode
+
+    def set_fusion(self, block_qubits: int, max_gates: int = 12) -> None:
+        """Dense-block fusion (0 = register-tile passes)."""
+        check(lib().qgpu_set_fusion(self._h, int(block_qubits), int(max_gates)), "qgpu_set_fusion")
 
     def close(self) -> None:
         if self._h:

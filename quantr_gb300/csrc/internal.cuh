@@ -45,6 +45,9 @@ struct qgpu_handle {
     int n_qubits = 0;
     int precision = QGPU_C128;
     int mode = QGPU_MODE_FAST;
+    int block_qubits = 0;      // > 0: fuse gates into dense blocks of this many wires
+    int block_gates = 12;      // at most this many gates per dense block
+    int batch_budget = 0;      // > 0: float-pair fusion budget picked by the batch autotuner
     int device = 0;
     int sm_count = 0;
     uint64_t dim = 0;          // 2^n amplitudes

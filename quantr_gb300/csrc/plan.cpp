@@ -684,4 +684,100 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
     return QGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Dense-block fusion
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+struct PendingGate {
+    int kg;
+    int bitpos[QGPU_MAX_OP_WIRES];  // full-index bit of gate wire m (gate-local bit kg-1-m)
+    std::vector<cd> E;              // column-major effective matrix (None rule folded in)
+};
+
+// Multiplies the pending gates, in order, into a dense matrix over their sorted bits.
+DenseBlock fuse_pending(const std::vector<PendingGate>& gs) {
+    DenseBlock b;
+    std::vector<int> bits;
+    for (const PendingGate& g : gs)
+        for (int m = 0; m < g.kg; ++m)
+            if (std::find(bits.begin(), bits.end(), g.bitpos[m]) == bits.end()) bits.push_back(g.bitpos[m]);
+    std::sort(bits.begin(), bits.end());
+    b.k = (int)bits.size();
+    for (int m = 0; m < b.k; ++m) b.bits[m] = bits[m];
+    const size_t D = (size_t)1 << b.k;
+    b.M.assign(D * D, cd(0, 0));
+    for (size_t i = 0; i < D; ++i) b.M[i * D + i] = 1.0;
+    std::vector<cd> col(D), out(D);
+    for (const PendingGate& g : gs) {
+        int lp[QGPU_MAX_OP_WIRES];  // block-local bit of gate wire m
+        for (int m = 0; m < g.kg; ++m)
+            lp[m] = (int)(std::find(bits.begin(), bits.end(), g.bitpos[m]) - bits.begin());
+        const size_t dg = (size_t)1 << g.kg;
+        size_t gmask = 0;
+        for (int m = 0; m < g.kg; ++m) gmask |= (size_t)1 << lp[m];
+        for (size_t c = 0; c < D; ++c) {  // new column c = G * (old column c)
+            for (size_t x = 0; x < D; ++x) col[x] = b.M[x * D + c];
+            std::fill(out.begin(), out.end(), cd(0, 0));
+            for (size_t x = 0; x < D; ++x) {
+                if (col[x] == cd(0, 0)) continue;
+                size_t j = 0;
+                for (int m = 0; m < g.kg; ++m) j = (j << 1) | ((x >> lp[m]) & 1u);
+                const size_t rest = x & ~gmask;
+                for (size_t l = 0; l < dg; ++l) {
+                    const cd e = g.E[j * dg + l];
+                    if (e == cd(0, 0)) continue;
+                    size_t y = rest;
+                    for (int m = 0; m < g.kg; ++m)
+                        if ((l >> (g.kg - 1 - m)) & 1u) y |= (size_t)1 << lp[m];
+                    out[y] += e * col[x];
+                }
+            }
+            for (size_t x = 0; x < D; ++x) b.M[x * D + c] = out[x];
+        }
+    }
+    b.gates = (int)gs.size();
+    return b;
+}
+
+}  // namespace
+
+int build_blocks(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
+                 const uint8_t* none, size_t n_none, int block_qubits, int max_gates,
+                 std::vector<DenseBlock>* out) {
+    out->clear();
+    std::vector<PendingGate> cur;
+    uint64_t cur_bits = 0;
+    auto flush = [&]() {
+        if (!cur.empty()) out->push_back(fuse_pending(cur));
+        cur.clear();
+        cur_bits = 0;
+    };
+    for (size_t g = 0; g < n_ops; ++g) {
+        if (ops[g].kind == QGPU_GATE_ID) continue;
+        LocalGate lg;
+        int st = tabulate(ops[g], n, mats, n_mats, none, n_none, &lg);
+        if (st != QGPU_OK) return st;
+        PendingGate pg;
+        pg.kg = lg.k;
+        uint64_t gb = 0;
+        for (int m = 0; m < lg.k; ++m) {
+            pg.bitpos[m] = n - 1 - lg.wires[m];
+            gb |= 1ull << pg.bitpos[m];
+        }
+        const size_t d = (size_t)1 << lg.k;
+        pg.E.resize(d * d);
+        for (size_t j = 0; j < d; ++j)
+            for (size_t l = 0; l < d; ++l)
+                pg.E[j * d + l] = lg.none[l] ? cd(l == j ? 1.0 : 0.0, 0.0)
+                                             : (lg.none[j] ? cd(0, 0) : lg.M[j * d + l]);
+        if (popcount64(cur_bits | gb) > std::max(block_qubits, lg.k) || (int)cur.size() >= max_gates)
+            flush();
+        cur.push_back(pg);
+        cur_bits |= gb;
+    }
+    flush();
+    return QGPU_OK;
+}
+
 }  // namespace qgpu

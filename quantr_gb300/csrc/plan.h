@@ -99,4 +99,19 @@ struct PlanOptions {
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
                const uint8_t* none, size_t n_none, const PlanOptions& opt, Plan* plan);
 
+// ---------------------------------------------------------------------------------------------
+// Dense-block fusion: consecutive gates whose wires fit in `block_qubits` wires (at most
+// `max_gates` of them) are multiplied on the host into one 2^k x 2^k complex matrix.
+// ---------------------------------------------------------------------------------------------
+struct DenseBlock {
+    int k = 0;
+    int bits[QGPU_MAX_OP_WIRES];       // full-index bit of local bit m (local bit 0 = bits[0])
+    std::vector<cd> M;                 // row-major: M[l * 2^k + j] = <l| U |j>
+    int gates = 0;
+};
+
+int build_blocks(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
+                 const uint8_t* none, size_t n_none, int block_qubits, int max_gates,
+                 std::vector<DenseBlock>* out);
+
 }  // namespace qgpu

@@ -685,7 +685,7 @@ static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, const float4* ta
 PlanOptions plan_options_for(const qgpu_handle* h) {
     PlanOptions o;
     o.policy = policy_of(h);
-    if (o.policy == POL_FF) o.budget = env_int("QGPU_FF_BUDGET", 140);
+    if (o.policy == POL_FF) o.budget = h->batch_budget > 0 ? h->batch_budget : env_int("QGPU_FF_BUDGET", 140);
     else if (o.policy == POL_F32) o.budget = env_int("QGPU_F32_BUDGET", 48);
     else o.budget = env_int("QGPU_F64_BUDGET", 1 << 20);
     o.max_bits = std::max(2, std::min(env_int("QGPU_TILE_BITS", MAX_TILE_BITS), MAX_TILE_BITS));
@@ -694,6 +694,9 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     o.max_arith_bits = o.policy == POL_FF ? env_int("QGPU_ARITH_TILE_BITS", 2) : MAX_TILE_BITS;
     return o;
 }
+
+int apply_blocks(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double* mats,
+                 size_t n_mats, const uint8_t* none, size_t n_none, int bq, int mg);  // blocks.cu
 
 // Runs non-Custom ops as fused passes on `buffer` (a state-sized device vector of the handle's
 // precision) instead of the register.
@@ -738,9 +741,21 @@ extern "C" int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_o
         }
         return QGPU_OK;
     }
+    if (h->block_qubits > 0)
+        return apply_blocks(h, ops, n_ops, mats, n_mat_doubles, none_flags, n_none_flags,
+                            h->block_qubits, h->block_gates);
     Plan plan;
     int st = build_plan(ops, n_ops, h->n_qubits, mats, n_mat_doubles, none_flags, n_none_flags,
                         plan_options_for(h), &plan);
     if (st != QGPU_OK) return st;
     return run_plan(h, plan);
+}
+
+extern "C" int qgpu_set_fusion(qgpu_handle* h, int block_qubits, int max_gates) {
+    if (!h) return fail(QGPU_ERR_INVALID, "qgpu_set_fusion: NULL handle");
+    if (block_qubits < 0 || block_qubits > 6 || max_gates < 1)
+        return fail(QGPU_ERR_INVALID, "qgpu_set_fusion: block_qubits must be 0..6 and max_gates >= 1");
+    h->block_qubits = block_qubits;
+    h->block_gates = max_gates;
+    return QGPU_OK;
 }
