@@ -182,6 +182,61 @@ def adjoint_leg(reps: int = 5) -> dict:
             "timer": "host wall clock around blocking calls"}
 
 
+def run_precision(args) -> None:
+    """Precision configuration (a secondary line, not the headline): the brickwork family on
+    complex64 at 33 qubits and complex128 at 32 qubits (64 GiB each), register-tile passes and
+    6-qubit dense blocks of up to 12 gates; and the 26-qubit cross-check of identical circuits
+    against the complex128 tile path (max |delta a|, 1 - fidelity, norm drift)."""
+    from quantr_gb300 import _native as nat
+    from quantr_gb300 import workloads as W
+
+    out = {"impl": "ours", "config": "precision", "cross_check_26q": {}, "full": {}}
+    prog26 = W.brickwork_qft(n=26, layers=20, seed=3)
+
+    def run26(precision, blocks):
+        h = nat.Handle(26, precision)
+        if blocks:
+            h.set_fusion(6, 12)
+        h.apply(prog26.ops, prog26.mats, prog26.none)
+        a = h.download()
+        nrm = h.norm()
+        h.close()
+        return a, nrm
+
+    ref, _ = run26(nat.QGPU_C128, 0)
+    for name, prec, blocks in [("c64_blocks", nat.QGPU_C64, 1), ("c64_tiles", nat.QGPU_C64, 0),
+                               ("c128_blocks", nat.QGPU_C128, 1)]:
+        a, nrm = run26(prec, blocks)
+        fid = abs(np.vdot(ref, a)) ** 2 / (np.vdot(a, a).real * np.vdot(ref, ref).real)
+        out["cross_check_26q"][name] = {"max_abs_err": float(np.max(np.abs(a - ref))),
+                                        "one_minus_fidelity": float(1.0 - fid),
+                                        "norm_drift": float(nrm - 1.0)}
+    peak = measured_peaks()["hbm_gbs"]
+    for n, prec, pname, block_layers in [(33, nat.QGPU_C64, "c64", 2), (32, nat.QGPU_C128, "c128", 1)]:
+        res = {}
+        for label, blocks, layers in [("tiles", 0, args.precision_layers), ("blocks", 1, block_layers)]:
+            prog = W.brickwork_qft(n=n, layers=layers, seed=3, qft=False)
+            h = nat.Handle(n, prec)
+            if blocks:
+                h.set_fusion(6, 12)
+            h.set_profiling(True)
+            h.profile(reset=True)
+            t0 = time.perf_counter()
+            h.apply(prog.ops, prog.mats, prog.none)
+            wall = time.perf_counter() - t0
+            prof = h.profile(reset=True)
+            nrm = h.norm()
+            h.close()
+            res[label] = {"layers": layers, "gates": int(len(prog.ops)), "wall_s": wall,
+                          "norm_drift": nrm - 1.0,
+                          "kernels": {k: {"launches": v[0], "ms_per_launch": v[1] / v[0],
+                                          "GBps": v[2] / (v[1] / 1e3) / 1e9,
+                                          "frac": v[2] / (v[1] / 1e3) / 1e9 / peak}
+                                      for k, v in prof.items()}}
+        out["full"][f"{n}q_{pname}"] = res
+    print(json.dumps(out), flush=True)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -373,7 +428,13 @@ def main() -> None:
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--ref-n", type=int, default=14)
     ap.add_argument("--ref-budget", type=float, default=15.0)
+    ap.add_argument("--config", choices=["headline", "precision"], default="headline",
+                    help="headline: the 30q c128 line; precision: the 33q c64 / 32q c128 leg")
+    ap.add_argument("--precision-layers", type=int, default=4)
     args = ap.parse_args()
+    if args.config == "precision":
+        run_precision(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
