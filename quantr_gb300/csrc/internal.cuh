@@ -54,6 +54,7 @@ struct qgpu_handle {
     size_t amp_bytes = 16;     // 16 (c128) or 8 (c64)
     void* state = nullptr;     // device amplitudes: double2[dim] or float2[dim]
     void* active = nullptr;    // when set, gate passes run on this buffer instead of `state`
+    int* d_err = nullptr;      // device error word of pipelined kernels (bounded waits)
     cudaStream_t stream = nullptr;
     qgpu::Scratch gates;       // per-program device tables (custom matrices, orders, flags)
     qgpu::Scratch tables;      // per-program phase tables of fused diagonal runs
@@ -167,6 +168,45 @@ __device__ __forceinline__ ffc to_ffc(double2 a) {
 }
 __device__ __forceinline__ double2 from_ffc(const ffc& a) {
     return make_double2(join_f64(a.rh, a.rl), join_f64(a.ih, a.il));
+}
+
+// ---- bulk copies (TMA, cp.async.bulk) with mbarrier completion -------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+// Global -> shared bulk copy; both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void fence_proxy_async_shared() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Bounded wait on an mbarrier phase: false after `limit` unsuccessful polls (each poll already
+// suspends the thread for a hardware-chosen interval).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
 }
 
 // ---- packed f32x2 arithmetic (Blackwell add/sub/mul/fma .rn.f32x2) ---------------------------

@@ -395,11 +395,12 @@ template <int K, int B, class P>
 __device__ __forceinline__ void step_on_bit(typename P::R* v, const DevStep& s, uint64_t base,
                                             const uint64_t* off) {
     constexpr int T = 1 << K;
+    const bool controlled = s.cm != 0;
 #pragma unroll
     for (int j = 0; j < T; ++j) {
         if ((j >> B) & 1) continue;
         const int j1 = j | (1 << B);
-        if (((base | off[j]) & s.cm) != s.cm) continue;
+        if (controlled && ((base | off[j]) & s.cm) != s.cm) continue;
         if (s.type == ST_PERM) {
             typename P::R a = v[j], b = v[j1];
             if (s.anti) {
@@ -491,7 +492,9 @@ __device__ __forceinline__ void step_tile(typename P::R* v, const DevStep& s, ui
     }
 }
 
-template <int K, int U, class P>
+// ONE >= 0: the pass is exactly one unconditional step of that type on tile bit 0 (the common
+// single fused gate), applied as straight-line code without the step loop or its dispatch.
+template <int K, int U, class P, int ONE = -1>
 __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, const __grid_constant__ TileParams p) {
     constexpr int T = 1 << K;
     uint64_t off[T];
@@ -525,10 +528,18 @@ __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, co
 #pragma unroll
             for (int j = 0; j < T; ++j) v[u][j] = P::load(raw[u][j]);
         // step-major: each step's constants and dispatch are read once for all U groups
-        for (int s = 0; s < p.nsteps; ++s) {
-            const DevStep& sp = p.steps[s];
+        if constexpr (ONE == ST_DENSE && IsArith<P>::value) {
 #pragma unroll
-            for (int u = 0; u < U; ++u) step_tile<K, P>(v[u], sp, base[u], off, p);
+            for (int u = 0; u < U; ++u) P::dense(v[u][0], v[u][1], p.steps[0]);
+        } else if constexpr (ONE == ST_REAL && IsArith<P>::value) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) P::real(v[u][0], v[u][1], p.steps[0]);
+        } else {
+            for (int s = 0; s < p.nsteps; ++s) {
+                const DevStep& sp = p.steps[s];
+#pragma unroll
+                for (int u = 0; u < U; ++u) step_tile<K, P>(v[u], sp, base[u], off, p);
+            }
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -540,6 +551,126 @@ __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, co
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// k_tile1_pipe: the 1-bit tile pass with bulk-copy (TMA) staging.
+// The register is cut into chunks of PIPE_CH amplitude pairs (32 KB of complex128). Chunk c of a
+// pass on bit q is either one contiguous run of 2*PIPE_CH amplitudes (q < log2 PIPE_CH: both
+// halves of every pair interleave inside it) or two runs of PIPE_CH amplitudes 2^q apart. Each
+// persistent CTA owns chunks blockIdx.x + i*gridDim.x; one thread keeps PIPE_STAGES-1 chunks in
+// flight with cp.async.bulk (mbarrier completion) while all threads compute the current chunk
+// from shared memory and store results straight to global memory (coalesced).
+// ---------------------------------------------------------------------------------------------
+constexpr int PIPE_LOG_CH = 10;
+constexpr int PIPE_CH = 1 << PIPE_LOG_CH;  // amplitude pairs per chunk
+constexpr int PIPE_STAGES = 2;
+constexpr int PIPE_THREADS = 256;
+constexpr uint32_t PIPE_WAIT_LIMIT = 1u << 24;  // polls before a wait is declared failed
+
+template <class P>
+__global__ void __launch_bounds__(PIPE_THREADS, 3)
+k_tile1_pipe(typename P::S* __restrict__ st, const __grid_constant__ TileParams p, uint64_t nchunks,
+             int* __restrict__ err) {
+    using S = typename P::S;
+    extern __shared__ __align__(128) unsigned char smem[];
+    S* stage = reinterpret_cast<S*>(smem);
+    __shared__ __align__(8) uint64_t bars[PIPE_STAGES];
+    const int q = p.bits[0];
+    const bool two_runs = q >= PIPE_LOG_CH;
+    const uint32_t chunk_bytes = 2u * PIPE_CH * (uint32_t)sizeof(S);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < PIPE_STAGES; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        fence_proxy_async_shared();
+    }
+    __syncthreads();
+    const uint64_t my_n =
+        nchunks > blockIdx.x ? (nchunks - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    auto chunk_of = [&](uint64_t i) -> uint64_t { return blockIdx.x + i * gridDim.x; };
+    auto issue = [&](uint64_t i, int s) {  // thread 0 only
+        const uint64_t c = chunk_of(i);
+        const uint32_t dst = smem_u32(stage + (size_t)s * 2 * PIPE_CH);
+        const uint32_t bar = smem_u32(&bars[s]);
+        mbar_arrive_expect_tx(bar, chunk_bytes);
+        if (two_runs) {
+            const uint64_t b0 = insert_zero(c * PIPE_CH, q);
+            bulk_g2s(dst, st + b0, chunk_bytes / 2, bar);
+            bulk_g2s(dst + chunk_bytes / 2, st + b0 + (1ull << q), chunk_bytes / 2, bar);
+        } else {
+            bulk_g2s(dst, st + c * 2 * PIPE_CH, chunk_bytes, bar);
+        }
+    };
+    if (threadIdx.x == 0)
+        for (int s = 0; s < PIPE_STAGES && (uint64_t)s < my_n; ++s) issue(s, s);
+    uint64_t off[2] = {0, 1ull << q};
+    bool failed = false;
+    uint64_t i = 0;
+    for (; i < my_n; ++i) {
+        const int s = (int)(i % PIPE_STAGES);
+        if (i > 0) {
+            __syncthreads();  // every thread is done with chunk i-1: refill its stage
+            if (threadIdx.x == 0 && i - 1 + PIPE_STAGES < my_n)
+                issue(i - 1 + PIPE_STAGES, (int)((i - 1) % PIPE_STAGES));
+        }
+        const bool ok = mbar_wait_bounded(smem_u32(&bars[s]), (uint32_t)((i / PIPE_STAGES) & 1),
+                                          PIPE_WAIT_LIMIT);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        const S* src = stage + (size_t)s * 2 * PIPE_CH;
+        const uint64_t c = chunk_of(i);
+#pragma unroll
+        for (int k = 0; k < PIPE_CH / PIPE_THREADS; ++k) {
+            const int lp = threadIdx.x + k * PIPE_THREADS;  // pair within the chunk
+            int l0, l1;
+            uint64_t g0;
+            if (two_runs) {
+                l0 = lp;
+                l1 = PIPE_CH + lp;
+                g0 = insert_zero(c * PIPE_CH, q) + lp;
+            } else {
+                l0 = (int)insert_zero((uint64_t)lp, q);
+                l1 = l0 + (1 << q);
+                g0 = c * 2 * PIPE_CH + l0;
+            }
+            typename P::R v[2] = {P::load(src[l0]), P::load(src[l1])};
+            for (int t = 0; t < p.nsteps; ++t) step_tile<1, P>(v, p.steps[t], g0, off, p);
+            st[g0] = P::store(v[0]);
+            st[g0 + (1ull << q)] = P::store(v[1]);
+        }
+    }
+    if (failed) {
+        // record the failure, then let this CTA's copies still in flight land before exiting
+        if (threadIdx.x == 0) {
+            atomicExch(err, 1);
+            for (uint64_t j = i; j < my_n && j < i + PIPE_STAGES; ++j)
+                mbar_wait_bounded(smem_u32(&bars[j % PIPE_STAGES]), (uint32_t)((j / PIPE_STAGES) & 1),
+                                  PIPE_WAIT_LIMIT);
+        }
+        __syncthreads();
+    }
+}
+
+template <class P>
+static int launch_tile1_pipe(qgpu_handle* h, const TileParams& p) {
+    using S = typename P::S;
+    const size_t smem = (size_t)PIPE_STAGES * 2 * PIPE_CH * sizeof(S);
+    static bool attr = false;
+    if (!attr) {
+        QGPU_CUDA(cudaFuncSetAttribute(k_tile1_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+        attr = true;
+    }
+    const uint64_t nchunks = h->dim / (2ull * PIPE_CH);
+    uint64_t blocks = std::min<uint64_t>(nchunks, (uint64_t)h->sm_count * 3);
+    if (blocks < 1) blocks = 1;
+    k_tile1_pipe<P><<<(unsigned)blocks, PIPE_THREADS, smem, h->stream>>>(
+        (S*)cur_state(h), p, nchunks, h->d_err);
+    QGPU_CHECK_LAUNCH("k_tile1_pipe");
+    h->launches++;
+    h->h2d_bytes += sizeof(TileParams);
+    return QGPU_OK;
+}
+
 template <int K, int U, class P>
 static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
     const uint64_t per_block = 256ull * U;
@@ -547,7 +678,20 @@ static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
     const uint64_t cap = (uint64_t)h->sm_count * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    k_tile<K, U, P><<<(unsigned)blocks, 256, 0, h->stream>>>((typename P::S*)cur_state(h), p);
+    typename P::S* s = (typename P::S*)cur_state(h);
+    bool launched = false;
+    if constexpr (K == 1 && IsArith<P>::value) {
+        if (p.nsteps == 1 && p.steps[0].cm == 0) {
+            if (p.steps[0].type == ST_DENSE) {
+                k_tile<K, U, P, ST_DENSE><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+                launched = true;
+            } else if (p.steps[0].type == ST_REAL) {
+                k_tile<K, U, P, ST_REAL><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+                launched = true;
+            }
+        }
+    }
+    if (!launched) k_tile<K, U, P><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
     QGPU_CHECK_LAUNCH("k_tile");
     h->launches++;
     h->h2d_bytes += sizeof(TileParams);
@@ -562,8 +706,13 @@ static int launch_tile_k(qgpu_handle* h, const TileParams& p) {
     // passes near 56 registers and 4 CTAs per SM; measured on GB300, 2 groups of a 1-bit tile
     // ran 17 % faster than 4.
     static const int k1_groups = env_int("QGPU_K1_GROUPS", 2);  // tuning knob: 2 or 4
+    // Bulk-copy staging for 1-bit tiles (k_tile1_pipe): correct and measured, but on GB300 its
+    // shared-memory footprint lowers occupancy below what the float-pair arithmetic needs, so the
+    // register-tile kernel stays the default (QGPU_PIPE=1 selects the pipeline).
+    static const int use_pipe = env_int("QGPU_PIPE", 0);
     switch (p.nbits) {
         case 1:
+            if (use_pipe && h->n_qubits >= 13) return launch_tile1_pipe<P>(h, p);
             return k1_groups == 4 ? launch_tile_t<1, 4, P>(h, p) : launch_tile_t<1, 2, P>(h, p);
         case 2: return launch_tile_t<2, 1, P>(h, p);
         default: return launch_tile_t<3, 1, P>(h, p);
@@ -630,6 +779,7 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         if (st != QGPU_OK) return st;
     }
     static const char* pol_name[] = {"ff", "f64", "f32"};
+    QGPU_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     for (size_t pi = 0; pi < plan.passes.size(); ++pi) {
         const Pass& ps = plan.passes[pi];
         if (h->profile) {
@@ -651,9 +801,12 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         if (st != QGPU_OK) return st;
         if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * pi + 1], h->stream));
     }
-    if (h->profile) return prof_collect(h, prof_names, prof_bytes);
+    int err = 0;
+    QGPU_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    int st = h->profile ? prof_collect(h, prof_names, prof_bytes) : QGPU_OK;
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
-    return QGPU_OK;
+    if (err) return fail(QGPU_ERR_TIMEOUT, "a pipelined pass gave up waiting for its bulk copies");
+    return st;
 }
 
 static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, const float4* tab_ff,

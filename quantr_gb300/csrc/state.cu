@@ -289,6 +289,12 @@ int qgpu_create(int n_qubits, int precision, qgpu_handle** out) {
         delete h;
         return cuda_fail(e, "cudaStreamCreateWithFlags");
     }
+    e = cudaMalloc(&h->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
+    if (e != cudaSuccess) {
+        qgpu_destroy(h);
+        return cuda_fail(e, "cudaMalloc(error word)");
+    }
     int st = qgpu_set_zero(h);
     if (st != QGPU_OK) {
         qgpu_destroy(h);
@@ -306,6 +312,7 @@ int qgpu_destroy(qgpu_handle* h) {
     h->work.release();
     h->work2.release();
     for (cudaEvent_t e : h->events) cudaEventDestroy(e);
+    if (h->d_err) cudaFree(h->d_err);
     if (h->state) cudaFree(h->state);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
