@@ -237,6 +237,41 @@ def run_precision(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_batch_leg(args) -> None:
+    """Batching configuration (a secondary line): independent ansatz circuits of 10..24 qubits,
+    4 layers each, own angles and observables; energies + adjoint gradients for every circuit in
+    one qgpu_batch_run call. Reports circuits/s and the fusion budget tuned per size bucket."""
+    from quantr_gb300 import _native as nat
+    from quantr_gb300 import batch as B
+    from quantr_gb300 import gradients as GR
+
+    cs = B.batch_config(count=args.batch_count)
+    sizes = {}
+    for c in cs:
+        sizes[c.n] = sizes.get(c.n, 0) + 1
+    out = {"impl": "ours", "config": "batch", "circuits": len(cs), "qubits_histogram": sizes,
+           "results": {}}
+    for pname, prec in (("c128", nat.QGPU_C128), ("c64", nat.QGPU_C64)):
+        B.run_batch(cs[:8], precision=prec)  # warm-up (module load, graph path)
+        t0 = time.perf_counter()
+        e, g, tuned = B.run_batch(cs, precision=prec)
+        dt = time.perf_counter() - t0
+        out["results"][pname] = {"seconds": dt, "circuits_per_s": len(cs) / dt,
+                                 "tuned_ff_budget_per_qubits": tuned,
+                                 "small_circuits_in_shared_memory": sum(
+                                     1 for c in cs if c.n <= (12 if pname == "c128" else 13))}
+        if pname == "c128":
+            rng = np.random.default_rng(0)
+            worst = 0.0
+            for i in rng.choice(len(cs), size=8, replace=False):
+                h = nat.Handle(cs[i].n)
+                ei, gi = GR.energy_and_gradient(h, cs[i].program, cs[i].a, cs[i].b)
+                h.close()
+                worst = max(worst, abs(ei - e[i]), float(np.max(np.abs(gi - g[i]))))
+            out["results"][pname]["max_abs_diff_vs_single_circuit_adjoint"] = worst
+    print(json.dumps(out), flush=True)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -428,12 +463,17 @@ def main() -> None:
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--ref-n", type=int, default=14)
     ap.add_argument("--ref-budget", type=float, default=15.0)
-    ap.add_argument("--config", choices=["headline", "precision"], default="headline",
-                    help="headline: the 30q c128 line; precision: the 33q c64 / 32q c128 leg")
+    ap.add_argument("--config", choices=["headline", "precision", "batch"], default="headline",
+                    help="headline: the 30q c128 line; precision: 33q c64 / 32q c128; batch: "
+                         "4096 circuits of 10..24 qubits")
     ap.add_argument("--precision-layers", type=int, default=4)
+    ap.add_argument("--batch-count", type=int, default=4096)
     args = ap.parse_args()
     if args.config == "precision":
         run_precision(args)
+        return
+    if args.config == "batch":
+        run_batch_leg(args)
         return
     if args.impl == "reference":
         run_reference(args)

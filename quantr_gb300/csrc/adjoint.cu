@@ -125,6 +125,50 @@ k_adj_1q(double2* __restrict__ phi, double2* __restrict__ lam, uint64_t npairs,
     if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
 }
 
+// The same sweep step for QGPU_MODE_FAST: the gradient term stays f64 (4 FMAs per pair on the
+// loaded doubles) while phi and lambda are updated with float-pair arithmetic (packed Dot2).
+struct AdjStepFF {
+    int t;
+    int gen;
+    u64 pk[32];  // ST_DENSE packed constants of V = U^dagger
+};
+
+__global__ void __launch_bounds__(ADJ_THREADS)
+k_adj_1q_ff(double2* __restrict__ phi, double2* __restrict__ lam, uint64_t npairs,
+            const __grid_constant__ AdjStepFF s, double* __restrict__ partial) {
+    __shared__ double sh[ADJ_THREADS];
+    double acc = 0.0;
+    for (uint64_t p = blockIdx.x * (uint64_t)ADJ_THREADS + threadIdx.x; p < npairs;
+         p += (uint64_t)gridDim.x * ADJ_THREADS) {
+        const uint64_t i0 = insert_zero(p, s.t), i1 = i0 | (1ull << s.t);
+        const double2 f0 = phi[i0], f1 = phi[i1], l0 = lam[i0], l1 = lam[i1];
+        switch (s.gen) {
+            case 1: acc += fma(l0.x, f1.y, -l0.y * f1.x) + fma(l1.x, f0.y, -l1.y * f0.x); break;
+            case 2: acc += fma(l1.x, f0.x, l1.y * f0.y) - fma(l0.x, f1.x, l0.y * f1.y); break;
+            case 3: acc += fma(l0.x, f0.y, -l0.y * f0.x) - fma(l1.x, f1.y, -l1.y * f1.x); break;
+            case 4: acc -= fma(l0.x, f0.y, -l0.y * f0.x) + fma(l1.x, f1.y, -l1.y * f1.x); break;
+            default: break;
+        }
+        ffp a = to_ffp(f0), b = to_ffp(f1);
+        ff_dense(a, b, s.pk);
+        phi[i0] = from_ffp(a);
+        phi[i1] = from_ffp(b);
+        a = to_ffp(l0);
+        b = to_ffp(l1);
+        ff_dense(a, b, s.pk);
+        lam[i0] = from_ffp(a);
+        lam[i1] = from_ffp(b);
+    }
+    if (!partial) return;
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = ADJ_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
 // grads[g] = sum over blocks of partial[g * nb + b], for g in [0, ng)
 __global__ void k_sum_partials(const double* __restrict__ partial, int nb, int ng,
                                double* __restrict__ out) {
@@ -300,8 +344,19 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
                 s.v[2 * (2 * l + j) + 1] = lg.M[j * 2 + l].imag();
             }
         double* part = rot_slot[gi] >= 0 ? partial + (size_t)rot_slot[gi] * nb : nullptr;
-        k_adj_1q<<<nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, h->dim / 2, s, part);
-        QGPU_CHECK_LAUNCH("k_adj_1q");
+        if (h->mode == QGPU_MODE_FAST) {
+            AdjStepFF f;
+            f.t = s.t;
+            f.gen = s.gen;
+            const cd v00(s.v[0], s.v[1]), v01(s.v[2], s.v[3]), v10(s.v[4], s.v[5]), v11(s.v[6], s.v[7]);
+            const DevStep ds = dense_step(v00, v01, v10, v11);
+            std::memcpy(f.pk, ds.pk, sizeof(f.pk));
+            k_adj_1q_ff<<<nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, h->dim / 2, f, part);
+            QGPU_CHECK_LAUNCH("k_adj_1q_ff");
+        } else {
+            k_adj_1q<<<nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, h->dim / 2, s, part);
+            QGPU_CHECK_LAUNCH("k_adj_1q");
+        }
         h->launches++;
     }
     st = flush_seg();

@@ -293,6 +293,26 @@ struct PDot2 {
     }
 };
 
+// (a, b) <- (u00 a + u01 b, u10 a + u11 b) with the packed Dot2 terms c[0..31] (DevStep::pk of an
+// ST_DENSE step): each output's real and imaginary lanes come from one 4-term Dot2.
+__device__ __forceinline__ void ff_dense(ffp& a, ffp& b, const u64* c) {
+    const u64 ash = pswap(a.h), asl = pswap(a.l), bsh = pswap(b.h), bsl = pswap(b.l);
+    PDot2 d;
+    ffp o0, o1;
+    d.first(c + 0, a.h, a.l);
+    d.add(c + 4, ash, asl);
+    d.add(c + 8, b.h, b.l);
+    d.add(c + 12, bsh, bsl);
+    d.result(o0.h, o0.l);
+    d.first(c + 16, a.h, a.l);
+    d.add(c + 20, ash, asl);
+    d.add(c + 24, b.h, b.l);
+    d.add(c + 28, bsh, bsl);
+    d.result(o1.h, o1.l);
+    a = o0;
+    b = o1;
+}
+
 // Accurate dot product accumulator (Ogita, Rump & Oishi 2005, "Dot2"): s carries the running
 // sum of the leading products, e collects every rounding error plus the small cross products.
 struct Dot2 {

@@ -466,6 +466,17 @@ bool fold_table(const std::vector<HStep>& run, Plan* plan, HStep* out) {
 
 }  // namespace
 
+DevStep dense_step(cd u00, cd u01, cd u10, cd u11) {
+    DevStep s = blank_step(ST_DENSE);
+    set_entry(s, 0, u00);
+    set_entry(s, 1, u01);
+    set_entry(s, 2, u10);
+    set_entry(s, 3, u11);
+    const cd e[4] = {u00, u01, u10, u11};
+    set_packed(s, e);
+    return s;
+}
+
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
                const uint8_t* none, size_t n_none, const PlanOptions& opt, Plan* plan) {
     plan->passes.clear();

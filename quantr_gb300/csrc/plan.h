@@ -99,6 +99,10 @@ struct PlanOptions {
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
                const uint8_t* none, size_t n_none, const PlanOptions& opt, Plan* plan);
 
+// An unconditional ST_DENSE step for out0 = u00 a + u01 b, out1 = u10 a + u11 b (all constant
+// forms filled in).
+DevStep dense_step(cd u00, cd u01, cd u10, cd u11);
+
 // ---------------------------------------------------------------------------------------------
 // Dense-block fusion: consecutive gates whose wires fit in `block_qubits` wires (at most
 // `max_gates` of them) are multiplied on the host into one 2^k x 2^k complex matrix.

@@ -258,22 +258,7 @@ struct PolFF {
     static __device__ __forceinline__ S store(const R& r) { return from_ffp(r); }
     // out0 = u00 a + u01 b ; out1 = u10 a + u11 b (packed terms, DevStep::pk)
     static __device__ __forceinline__ void dense(R& a, R& b, const DevStep& s) {
-        const u64* c = s.pk;
-        const u64 ash = pswap(a.h), asl = pswap(a.l), bsh = pswap(b.h), bsl = pswap(b.l);
-        PDot2 d;
-        R o0, o1;
-        d.first(c + 0, a.h, a.l);
-        d.add(c + 4, ash, asl);
-        d.add(c + 8, b.h, b.l);
-        d.add(c + 12, bsh, bsl);
-        d.result(o0.h, o0.l);
-        d.first(c + 16, a.h, a.l);
-        d.add(c + 20, ash, asl);
-        d.add(c + 24, b.h, b.l);
-        d.add(c + 28, bsh, bsl);
-        d.result(o1.h, o1.l);
-        a = o0;
-        b = o1;
+        ff_dense(a, b, s.pk);
     }
     static __device__ __forceinline__ void real(R& a, R& b, const DevStep& s) {
         const u64* c = s.pk;
