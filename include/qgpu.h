@@ -157,6 +157,14 @@ int qgpu_measure_uniforms(qgpu_handle* h, const double* u, size_t n, int64_t* ou
  * the GPU (other handles' streams on the same device) race. */
 int qgpu_measure_uniforms_noalloc(qgpu_handle* h, const double* u, size_t n, int64_t* out);
 
+/* `SuperPosition::to_hash_map` (src/circuit/states/super_positions.rs:315-323) without a full
+ * download: the indices and amplitudes (interleaved re, im) of every amplitude whose |a|^2 is
+ * not within `margin` of 0 (quantr uses 1e-6), in increasing index order. *count receives the
+ * number of survivors; when it exceeds `cap`, the first `cap` are written and QGPU_ERR_INVALID is
+ * returned. */
+int qgpu_extract_nonzero(qgpu_handle* h, double margin, uint64_t* idx_out, double* amp_out,
+                         size_t cap, size_t* count);
+
 /* f64 reductions of the state: sum |a_i|^2, and the amplitude checksum sum a_i. */
 int qgpu_norm(qgpu_handle* h, double* out);
 int qgpu_checksum(qgpu_handle* h, double* re_out, double* im_out);
@@ -201,6 +209,11 @@ int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, const qgpu_op* 
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or order work on it. */
 void* qgpu_stream(qgpu_handle* h);
+/* Failure-detection check: one CTA polls, at most `polls` times (1..2^20), an mbarrier phase
+ * that nothing completes, the same bounded wait the pipelined passes use. Returns
+ * QGPU_ERR_TIMEOUT with the device error word recorded and cleared; the context stays usable. */
+int qgpu_selftest_bounded_wait(qgpu_handle* h, uint32_t polls);
+
 /* Number of kernels this handle has launched since creation. */
 uint64_t qgpu_launch_count(const qgpu_handle* h);
 /* Bytes this handle has moved host->device (copies and kernel parameters) and device->host. */

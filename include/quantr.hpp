@@ -275,6 +275,19 @@ class SimulatedCircuit {
         return {false, SuperPosition(std::move(a), num_qubits_)};
     }
     Measurement<SuperPosition> take_state() const { return get_state(); }
+    // get_state().take().to_hash_map() computed on the device: only survivors are copied back.
+    std::map<ProductState, Complex64> state_hash_map(double margin = 1e-6) const {
+        size_t n = 0;
+        int st = qgpu_extract_nonzero(handle_.get(), margin, nullptr, nullptr, 0, &n);
+        if (st != QGPU_OK && st != QGPU_ERR_INVALID) check(st);
+        std::vector<uint64_t> idx(n ? n : 1);
+        std::vector<Complex64> amp(n ? n : 1);
+        check(qgpu_extract_nonzero(handle_.get(), margin, idx.data(),
+                                   reinterpret_cast<double*>(amp.data()), n, &n));
+        std::map<ProductState, Complex64> m;
+        for (size_t i = 0; i < n; ++i) m[ProductState::binary_basis(idx[i], num_qubits_)] = amp[i];
+        return m;
+    }
     void print_warnings(bool printing) { disable_warnings_ = printing; }
     const std::vector<Gate>& get_circuit_gates() const { return circuit_gates_; }
     size_t get_num_qubits() const { return num_qubits_; }

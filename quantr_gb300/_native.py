@@ -63,12 +63,15 @@ _EXPORTS = {
                                C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_uint64)]),
     "qgpu_measure_uniforms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "qgpu_measure_uniforms_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "qgpu_extract_nonzero": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_size_t,
+                                       C.POINTER(C.c_size_t)]),
     "qgpu_norm": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "qgpu_checksum": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "qgpu_expectation_zzx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "qgpu_adjoint_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
                                     C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
                                     C.POINTER(C.c_double), C.c_void_p]),
+    "qgpu_selftest_bounded_wait": (C.c_int, [C.c_void_p, C.c_uint32]),
     "qgpu_stream": (C.c_void_p, [C.c_void_p]),
     "qgpu_launch_count": (C.c_uint64, [C.c_void_p]),
     "qgpu_io_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
@@ -184,6 +187,20 @@ class Handle:
         check(lib().qgpu_measure_uniforms(self._h, ptr(u), u.size, ptr(out)),
               "qgpu_measure_uniforms")
         return out
+
+    def extract_nonzero(self, margin: float = 1e-6, cap: int | None = None):
+        """(indices, amplitudes) of |a|^2 not within `margin` of 0, ascending index order."""
+        cnt = C.c_size_t()
+        if cap is None:  # count first, then fetch exactly that many
+            st = lib().qgpu_extract_nonzero(self._h, float(margin), None, None, 0, C.byref(cnt))
+            if st not in (QGPU_OK, QGPU_ERR_INVALID):
+                check(st, "qgpu_extract_nonzero")
+            cap = cnt.value
+        idx = np.empty(max(cap, 1), dtype=np.uint64)
+        amp = np.empty(max(cap, 1), dtype=np.complex128)
+        check(lib().qgpu_extract_nonzero(self._h, float(margin), ptr(idx), ptr(amp), cap,
+                                         C.byref(cnt)), "qgpu_extract_nonzero")
+        return idx[:cnt.value].copy(), amp[:cnt.value].copy()
 
     def norm(self) -> float:
         v = C.c_double()

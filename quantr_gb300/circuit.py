@@ -18,7 +18,7 @@ from . import rng
 from .errors import QuantrError
 from .gate import Gate
 from .program import lower
-from .states import ProductState, SuperPosition
+from .states import ZERO_MARGIN, ProductState, SuperPosition
 
 _DEFAULTS = {"precision": nat.QGPU_C128, "mode": nat.QGPU_MODE_FAST}
 _PRECISION = {"c128": nat.QGPU_C128, "c64": nat.QGPU_C64}
@@ -317,6 +317,14 @@ class SimulatedCircuit:
 
     def take_state(self) -> NonObservable:
         return NonObservable(self._register())
+
+    def state_hash_map(self, margin: float = ZERO_MARGIN) -> dict:
+        """`get_state().take().to_hash_map()` (super_positions.rs:315-323) computed on the device:
+        only the surviving amplitudes cross PCIe/C2C, so a sparse 30-qubit register needs no
+        16 GiB download."""
+        idx, amp = self._handle.extract_nonzero(margin)
+        return {ProductState.binary_basis(int(i), self.num_qubits): complex(a)
+                for i, a in zip(idx, amp)}
 
     def print_warnings(self, printing: bool) -> None:
         # simulated_circuit.rs:163-165: the flag is stored as `disable_warnings`

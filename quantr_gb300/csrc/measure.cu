@@ -261,11 +261,120 @@ static int run_sample(qgpu_handle* h, const Cdf& c, const double* u, uint64_t n,
     return QGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Sparse extraction (`SuperPosition::to_hash_map`, super_positions.rs:315-323): amplitudes whose
+// |a|^2 is not within `margin` of zero, in increasing index order. Per 512-amplitude chunk:
+// count (k_nz_count), exclusive scan of the counts (scan_exclusive), then each chunk writes its
+// survivors at its offset with a warp ballot + popcount order (k_nz_write).
+// ---------------------------------------------------------------------------------------------
+template <class S>
+__global__ void k_nz_count(const S* __restrict__ st, uint64_t nchunks, int chunk_len, double margin,
+                           double* __restrict__ counts) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t c = warp; c < nchunks; c += nwarps) {
+        unsigned cnt = 0;
+        for (int q = lane; q < chunk_len; q += 32) {
+            const double p = prob(st, c * (uint64_t)chunk_len + q);
+            cnt += !(p > -margin && p < margin);
+        }
+        for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, d);
+        if (lane == 0) counts[c] = (double)cnt;
+    }
+}
+
+template <class S>
+__global__ void k_nz_write(const S* __restrict__ st, uint64_t nchunks, int chunk_len, double margin,
+                           const double* __restrict__ offs, uint64_t cap,
+                           uint64_t* __restrict__ idx, double2* __restrict__ amp) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t c = warp; c < nchunks; c += nwarps) {
+        uint64_t at = (uint64_t)offs[c];
+        for (int q0 = 0; q0 < chunk_len; q0 += 32) {
+            const int q = q0 + lane;
+            bool keep = false;
+            double2 a = make_double2(0, 0);
+            const uint64_t i = c * (uint64_t)chunk_len + q;
+            if (q < chunk_len) {
+                a = make_double2((double)st[i].x, (double)st[i].y);
+                const double p = __dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y));
+                keep = !(p > -margin && p < margin);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            const uint64_t pos = at + __popc(m & ((1u << lane) - 1u));
+            if (keep && pos < cap) {
+                idx[pos] = i;
+                amp[pos] = a;
+            }
+            at += __popc(m);
+        }
+    }
+}
+
 }  // namespace qgpu
 
 using namespace qgpu;
 
 extern "C" {
+
+int qgpu_extract_nonzero(qgpu_handle* h, double margin, uint64_t* idx_out, double* amp_out,
+                         size_t cap, size_t* count) {
+    if (!h || !count || (cap && (!idx_out || !amp_out)))
+        return fail(QGPU_ERR_INVALID, "qgpu_extract_nonzero: NULL argument");
+    Cdf c;  // chunk geometry and scratch of the sampler; sums hold survivor counts here
+    const int cb = h->n_qubits < CHUNK_BITS ? h->n_qubits : CHUNK_BITS;
+    c.chunk_len = 1 << cb;
+    c.nchunks = h->dim >> cb;
+    const size_t tmp = scan_tmp_len(c.nchunks);
+    int st = h->work.ensure((c.nchunks + tmp + 4) * sizeof(double) + 256);
+    if (st != QGPU_OK) return st;
+    double* counts = (double*)h->work.ptr;
+    double* total = counts + c.nchunks;
+    double* scan_tmp = total + 2;
+    const int threads = 256;
+    uint64_t blocks = (c.nchunks * 32 + threads - 1) / threads;
+    if (blocks > (uint64_t)h->sm_count * 16) blocks = (uint64_t)h->sm_count * 16;
+    if (h->precision == QGPU_C128)
+        k_nz_count<double2><<<(unsigned)blocks, threads, 0, h->stream>>>(
+            (const double2*)h->state, c.nchunks, c.chunk_len, margin, counts);
+    else
+        k_nz_count<float2><<<(unsigned)blocks, threads, 0, h->stream>>>(
+            (const float2*)h->state, c.nchunks, c.chunk_len, margin, counts);
+    QGPU_CHECK_LAUNCH("k_nz_count");
+    h->launches++;
+    st = scan_exclusive(h, counts, c.nchunks, scan_tmp, total);  // counts -> offsets (exact:
+    if (st != QGPU_OK) return st;                                 // integers below 2^53)
+    double tot = 0.0;
+    QGPU_CUDA(copy_async(h, &tot, total, sizeof(double), cudaMemcpyDeviceToHost));
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    const uint64_t n = (uint64_t)tot;
+    *count = (size_t)n;
+    const uint64_t keep = n < cap ? n : cap;
+    if (keep) {
+        st = h->work2.ensure(keep * 24 + 512);
+        if (st != QGPU_OK) return st;
+        uint64_t* d_idx = (uint64_t*)h->work2.ptr;
+        double2* d_amp = (double2*)((uint8_t*)h->work2.ptr + ((keep * 8 + 255) / 256) * 256);
+        if (h->precision == QGPU_C128)
+            k_nz_write<double2><<<(unsigned)blocks, threads, 0, h->stream>>>(
+                (const double2*)h->state, c.nchunks, c.chunk_len, margin, counts, keep, d_idx, d_amp);
+        else
+            k_nz_write<float2><<<(unsigned)blocks, threads, 0, h->stream>>>(
+                (const float2*)h->state, c.nchunks, c.chunk_len, margin, counts, keep, d_idx, d_amp);
+        QGPU_CHECK_LAUNCH("k_nz_write");
+        h->launches++;
+        QGPU_CUDA(copy_async(h, idx_out, d_idx, keep * 8, cudaMemcpyDeviceToHost));
+        QGPU_CUDA(copy_async(h, amp_out, d_amp, keep * 16, cudaMemcpyDeviceToHost));
+        QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    if (n > cap)
+        return fail(QGPU_ERR_INVALID, "qgpu_extract_nonzero: " + std::to_string(n) +
+                                          " amplitudes survive, cap is " + std::to_string(cap));
+    return QGPU_OK;
+}
 
 int qgpu_measure_uniforms(qgpu_handle* h, const double* u, size_t n, int64_t* out) {
     if (!h || (n && (!u || !out))) return fail(QGPU_ERR_INVALID, "qgpu_measure_uniforms: NULL argument");

@@ -659,6 +659,13 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
         cur_cost = 0;
         cur_arith = false;
     };
+    // controlled-X step (X, CNot, Toffoli as a PERM without phases)
+    auto is_cx = [&](size_t i) {
+        const HStep& h = steps[i];
+        return block_at[i] < 0 && h.s.type == ST_PERM && h.s.anti && h.s.u0 == 0 && h.s.u1 == 0 &&
+               h.need[0] >= 0;
+    };
+    auto is_sw = [&](size_t i) { return block_at[i] < 0 && steps[i].s.type == ST_SWAP; };
     for (size_t i = 0; i < steps.size(); ++i) {
         if (block_at[i] >= 0) {
             flush();
@@ -666,6 +673,77 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
             p.custom = block_at[i];
             plan->passes.push_back(p);
             continue;
+        }
+        if (opt.xor_runs && (is_cx(i) || is_sw(i))) {
+            // longest run of controlled-X / swap steps forming one involution
+            uint64_t targets = 0, controls = 0, swapped = 0;
+            size_t j = i;
+            while (j < steps.size() && (is_cx(j) || is_sw(j))) {
+                if (is_sw(j)) {
+                    const uint64_t sb = (1ull << steps[j].need[0]) | (1ull << steps[j].need[1]);
+                    if (sb & (targets | controls | swapped)) break;
+                    swapped |= sb;
+                } else {
+                    const uint64_t tb = 1ull << steps[j].need[0], cm = steps[j].s.cm;
+                    if ((targets & tb) || (targets & cm) || (controls & tb) || (swapped & (tb | cm)))
+                        break;
+                    targets |= tb;
+                    controls |= cm;
+                }
+                ++j;
+            }
+            XorPerm xp;
+            bool fits = j - i >= 3;
+            for (size_t q = i; q < j && fits; ++q) {
+                if (is_sw(q)) {
+                    if (xp.nterms == MAX_XOR_TERMS) { fits = false; break; }
+                    const int g = xp.nterms++;
+                    xp.grouped[g] = 2;
+                    xp.shift[g] = 0;
+                    xp.cm[g] = (1ull << steps[q].need[0]) | (1ull << steps[q].need[1]);
+                    xp.tbit[g] = 0;
+                    continue;
+                }
+                const int t = steps[q].need[0];
+                const uint64_t cm = steps[q].s.cm;
+                if (popcount64(cm) == 1) {
+                    const int c = __builtin_ctzll(cm);
+                    const int shift = c - t;
+                    int g = -1;
+                    for (int e = 0; e < xp.nterms; ++e)
+                        if (xp.grouped[e] && xp.shift[e] == shift) g = e;
+                    if (g < 0) {
+                        if (xp.nterms == MAX_XOR_TERMS) { fits = false; break; }
+                        g = xp.nterms++;
+                        xp.grouped[g] = 1;
+                        xp.shift[g] = shift;
+                        xp.cm[g] = 0;
+                        xp.tbit[g] = 0;
+                    }
+                    xp.cm[g] |= cm;
+                    xp.tbit[g] |= 1ull << t;
+                } else {
+                    if (xp.nterms == MAX_XOR_TERMS) { fits = false; break; }
+                    const int g = xp.nterms++;
+                    xp.grouped[g] = 0;
+                    xp.shift[g] = 0;
+                    xp.cm[g] = cm;
+                    xp.tbit[g] = 1ull << t;
+                }
+            }
+            if (fits) {
+                flush();
+                Pass p;
+                p.xor_pass = true;
+                p.xp = xp;
+                double touched = 0.0;
+                for (size_t q = i; q < j; ++q)
+                    touched += is_sw(q) ? 0.5 : std::ldexp(1.0, -popcount64(steps[q].s.cm));
+                p.touched = std::min(1.0, touched);
+                plan->passes.push_back(p);
+                i = j - 1;
+                continue;
+            }
         }
         const HStep& h = steps[i];
         std::vector<int> bits = cur_bits;

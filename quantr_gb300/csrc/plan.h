@@ -68,9 +68,26 @@ struct DevStep {
     uint64_t pk[32];
 };
 
+// A run of commuting controlled-X gates (X, CNot, Toffoli) and swaps whose targets are neither
+// controls nor each other's targets (a swap's two bits belong to no other gate of the run): the
+// run is the involution i -> i ^ f(i), with f built from terms. A grouped term (grouped = 1)
+// covers single-bit controls that sit `shift` bits above their targets: f |= ((i & cm) >> shift);
+// a plain term (0) is one gate: f |= tbit when (i & cm) == cm; a swap term (2) has cm = its two
+// bits: f |= cm when exactly one of them is set.
+constexpr int MAX_XOR_TERMS = 24;
+struct XorPerm {
+    int nterms = 0;
+    uint64_t cm[MAX_XOR_TERMS];
+    uint64_t tbit[MAX_XOR_TERMS];   // plain term: target bit mask
+    int shift[MAX_XOR_TERMS];       // grouped term: control = target + shift (shift > 0)
+    int grouped[MAX_XOR_TERMS];
+};
+
 struct Pass {
     int nbits = 0;                     // tile bits
     int bits[MAX_TILE_BITS];           // full-index bit positions, ascending
+    bool xor_pass = false;             // the pass is one XorPerm (k_xor_perm)
+    XorPerm xp;
     bool arith = false;                // needs float-pair / f64 arithmetic
     int cost = 0;                      // planner's ops-per-amplitude estimate
     double touched = 1.0;              // fraction of amplitudes the pass may change
@@ -94,6 +111,7 @@ struct PlanOptions {
     int budget = 100;                  // arithmetic ops per amplitude a pass may carry
     bool merge_1q = true;              // multiply runs of single-wire gates into one matrix
     bool fuse_diagonal = true;         // fold diagonal runs into phase tables
+    bool xor_runs = true;              // runs of >= 3 commuting controlled-X gates -> one pass
 };
 
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,

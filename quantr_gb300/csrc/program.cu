@@ -670,6 +670,51 @@ static int launch_tile1_pipe(qgpu_handle* h, const TileParams& p) {
     return QGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// k_xor_perm: a run of commuting controlled-X gates as one involution i -> j = i ^ f(i). f only
+// reads control bits, which no gate of the run changes, so f(j) = f(i): the thread with the
+// smaller index of each pair swaps it, the other does nothing. Amplitudes no gate moves are not
+// touched.
+// ---------------------------------------------------------------------------------------------
+template <class S>
+__global__ void __launch_bounds__(256) k_xor_perm(S* __restrict__ st, uint64_t dim,
+                                                  const __grid_constant__ XorPerm xp) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += stride) {
+        uint64_t f = 0;
+        for (int e = 0; e < xp.nterms; ++e) {
+            if (xp.grouped[e] == 1) {
+                const uint64_t c = i & xp.cm[e];
+                f |= xp.shift[e] > 0 ? (c >> xp.shift[e]) : (c << -xp.shift[e]);
+            } else if (xp.grouped[e] == 2) {
+                if (__popcll(i & xp.cm[e]) == 1) f |= xp.cm[e];  // swap of two differing bits
+            } else if ((i & xp.cm[e]) == xp.cm[e]) {
+                f |= xp.tbit[e];
+            }
+        }
+        const uint64_t j = i ^ f;
+        if (j > i) {
+            const S a = st[i], b = st[j];
+            st[i] = b;
+            st[j] = a;
+        }
+    }
+}
+
+static int launch_xor(qgpu_handle* h, const XorPerm& xp) {
+    uint64_t blocks = (h->dim + 255) / 256;
+    const uint64_t cap = (uint64_t)h->sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    if (h->precision == QGPU_C128)
+        k_xor_perm<double2><<<(unsigned)blocks, 256, 0, h->stream>>>((double2*)cur_state(h), h->dim, xp);
+    else
+        k_xor_perm<float2><<<(unsigned)blocks, 256, 0, h->stream>>>((float2*)cur_state(h), h->dim, xp);
+    QGPU_CHECK_LAUNCH("k_xor_perm");
+    h->launches++;
+    h->h2d_bytes += sizeof(XorPerm);
+    return QGPU_OK;
+}
+
 template <int K, int U, class P>
 static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
     const uint64_t per_block = 256ull * U;
@@ -785,6 +830,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
             QGPU_CUDA(cudaEventRecord(h->events[2 * pi], h->stream));
             if (ps.custom >= 0) {
                 prof_names.push_back("k_group");
+            } else if (ps.xor_pass) {
+                prof_names.push_back("k_xor_perm");
             } else {
                 prof_names.push_back(std::string("k_tile<") + std::to_string(ps.nbits) + "," +
                                      (ps.arith ? pol_name[pol] : "move") + ">");
@@ -794,6 +841,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         int st = QGPU_OK;
         if (ps.custom >= 0) {
             st = launch_group(h, gargs[ps.custom], (const uint8_t*)h->gates.ptr, lay[ps.custom]);
+        } else if (ps.xor_pass) {
+            st = launch_xor(h, ps.xp);
         } else {
             st = launch_pass(h, ps, pol, tab_ff, tab_f64, tp);
         }
@@ -905,6 +954,35 @@ extern "C" int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_o
                         plan_options_for(h), &plan);
     if (st != QGPU_OK) return st;
     return run_plan(h, plan);
+}
+
+// One CTA waits, with the pipelined kernels' bounded poll, on an mbarrier phase that nothing
+// completes; when the poll limit runs out it records the failure exactly as k_tile1_pipe does.
+__global__ void k_wait_selftest(uint32_t polls, int* err) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&bar), 1);
+        fence_proxy_async_shared();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(smem_u32(&bar), 0, polls);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+extern "C" int qgpu_selftest_bounded_wait(qgpu_handle* h, uint32_t polls) {
+    if (!h || polls == 0 || polls > (1u << 20))
+        return fail(QGPU_ERR_INVALID, "qgpu_selftest_bounded_wait: polls must be 1..2^20");
+    QGPU_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    k_wait_selftest<<<1, 32, 0, h->stream>>>(polls, h->d_err);
+    QGPU_CHECK_LAUNCH("k_wait_selftest");
+    h->launches++;
+    int err = 0;
+    QGPU_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    QGPU_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    if (err) return fail(QGPU_ERR_TIMEOUT, "bounded wait gave up after " + std::to_string(polls) + " polls");
+    return QGPU_OK;
 }
 
 extern "C" int qgpu_set_fusion(qgpu_handle* h, int block_qubits, int max_gates) {

@@ -138,6 +138,18 @@ int main() {
         std::printf("%s pushes_multi_gates\n", ok ? "PASS" : "FAIL");
         if (!ok) ++failures;
     }
+    {  // device-side to_hash_map equals the host rule on the downloaded register
+        Circuit c = Circuit::new_(10);
+        c.add_gate(Gate::H(), 0);
+        for (size_t t = 1; t < 10; ++t) c.add_gate(Gate::CNot(0), t);
+        c.add_gate(Gate::Ry(0.7), 4);
+        auto sim = std::move(c).simulate();
+        auto dev = sim.state_hash_map();
+        auto host = sim.get_state().take().to_hash_map();
+        const bool ok = dev == host && dev.size() == 4;
+        std::printf("%s state_hash_map\n", ok ? "PASS" : "FAIL");
+        if (!ok) ++failures;
+    }
     expect_error("catches_overlapping_control_nodes",
                  [] { Circuit::new_(3).add_gates({Gate::CNot(0), Gate::Id(), Gate::Id()}); });
     expect_error("control_node_greater_than_circuit_size",

@@ -127,6 +127,37 @@ def test_every_gate_on_every_wire(oracle, mode):
         assert np.max(np.abs(out - ref)) <= TOL_FAST
 
 
+@pytest.mark.parametrize("precision", [nat.QGPU_C128, nat.QGPU_C64])
+def test_commuting_cx_runs(oracle, precision):
+    """Runs of commuting controlled-X gates (bricks with controls above and below the targets,
+    Toffolis, bare X) applied as one index involution per run."""
+    n = 11
+    rng = np.random.default_rng(8)
+    reg = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    reg /= np.linalg.norm(reg)
+    b = ProgramBuilder(n)
+    for i in range(0, n - 1, 2):
+        b.add("CNot", i + 1, (i,))         # control one wire above: control bit = target bit + 1
+    b.add("Ry", 3, (), param=0.4)
+    for i in range(1, n - 1, 2):
+        b.add("CNot", i, (i + 1,))         # control below the target
+    b.add("Toffoli", 10, (0, 4))
+    b.add("X", 2)
+    b.add("Toffoli", 6, (8, 1))
+    b.add("H", 5)
+    b.add("X", 0); b.add("CNot", 3, (7,)); b.add("X", 9); b.add("Toffoli", 4, (2, 6))
+    b.add("T", 1)
+    for i in range(4):                     # QFT-style swaps, then controlled-X on other wires
+        b.add("Swap", i, (n - 1 - i,))
+    b.add("CNot", 5, (4,))
+    b.add("Swap", 6, (5,))                  # overlaps the CNot: starts a new run
+    prog = b.build()
+    ref = oracle.simulate(prog, reg, engine=oracle.DENSE)
+    out = run_gpu(prog, "fast", precision=precision, reg=reg)
+    tol = TOL_FAST if precision == nat.QGPU_C128 else 1e-6
+    assert np.max(np.abs(out - ref)) <= tol
+
+
 @pytest.mark.parametrize("mode", ["exact", "fast"])
 def test_custom_blocks_dense_nonunitary_and_wide(oracle, mode):
     """Custom gates: a dense 3-wire block with None entries, a non-unitary block, and the widest
