@@ -11,6 +11,7 @@
 // a thrown quantr::QuantrError. Link with -lquantr_gpu.
 #pragma once
 
+#include <algorithm>
 #include <complex>
 #include <cstdint>
 #include <functional>
@@ -236,6 +237,59 @@ inline uint64_t& shot_seed() {
 // `fastrand::seed` counterpart: reseeds the stream that keys each measure_all call.
 inline void seed(uint64_t s) { shot_seed() = s; }
 
+// The flat gate list as a gate program (simulation.rs:37-56): `Id` skipped, wire = index % n,
+// every Custom tabulated by calling its function on each local basis state
+// (simulation.rs:137-156).
+struct Program {
+    std::vector<qgpu_op> ops;
+    std::vector<double> mats;
+    std::vector<uint8_t> none;
+};
+
+inline Program lower(const std::vector<Gate>& gates, size_t n, bool progress) {
+    Program p;
+    size_t counter = 0;
+    for (const Gate& g : gates) {
+        if (g.kind == QGPU_GATE_ID) {
+            ++counter;
+            continue;
+        }
+        qgpu_op op{};
+        op.kind = g.kind;
+        op.target = (int32_t)(counter % n);
+        op.n_controls = (int32_t)g.controls.size();
+        for (size_t m = 0; m < g.controls.size() && m < QGPU_MAX_OP_WIRES; ++m)
+            op.controls[m] = (int32_t)g.controls[m];
+        op.param = g.angle;
+        op.k = g.k;
+        if (g.is_custom_gate()) {
+            const size_t kq = g.controls.size() + 1, d = (size_t)1 << kq;
+            op.mat_offset = (int64_t)p.mats.size();
+            op.none_offset = (int64_t)p.none.size();
+            for (size_t j = 0; j < d; ++j) {
+                auto img = g.func(ProductState::binary_basis(j, kq));
+                p.none.push_back(img ? 0 : 1);
+                for (size_t l = 0; l < d; ++l) {
+                    Complex64 v = (img && l < img->amplitudes.size()) ? img->amplitudes[l] : 0.0;
+                    p.mats.push_back(v.real());
+                    p.mats.push_back(v.imag());
+                }
+            }
+        }
+        if (progress)
+            std::cout << "Applying gate " << g.kind << " on wire " << op.target << " # "
+                      << counter + 1 << "/" << gates.size() << " \n";
+        p.ops.push_back(op);
+        ++counter;
+    }
+    return p;
+}
+
+inline void apply(qgpu_handle* h, const Program& p) {
+    check(qgpu_apply_program(h, p.ops.data(), p.ops.size(), p.mats.data(), p.mats.size(),
+                             p.none.data(), p.none.size()));
+}
+
 class SimulatedCircuit {
    public:
     SimulatedCircuit(std::vector<Gate> g, size_t n, Handle h, bool progress)
@@ -267,6 +321,54 @@ class SimulatedCircuit {
             std::cerr << "\x1b[93m[Quantr Warning] The superposition failed to collapse to a "
                          "state during repeat measurements. This is likely due to the use of "
                          "Gate::Custom where the mapping is not unitary.\x1b[0m\n";
+        return {true, std::move(bins)};
+    }
+    // simulated_circuit.rs:81-114. Shot 1 from the cached register, later shots from a
+    // re-simulation from |0...0> with every Custom re-tabulated (a function drawing random Kraus
+    // branches gets a fresh draw per shot). Consecutive shots whose tables are identical share one
+    // re-simulation and one sampler call.
+    Measurement<std::map<ProductState, size_t>> measure_all_without_cache(size_t shots) {
+        if (shots == 0) throw QuantrError("measure_all_without_cache needs at least one shot.");
+        std::map<ProductState, size_t> bins;
+        auto add = [&](size_t count) {
+            const size_t cap = std::min<size_t>(count, (size_t)1 << std::min<size_t>(num_qubits_, 40));
+            std::vector<uint64_t> idx(cap ? cap : 1), cnt(cap ? cap : 1);
+            size_t nu = 0;
+            uint64_t failed = 0;
+            shot_seed() = shot_seed() * 6364136223846793005ull + 1442695040888963407ull;
+            check(qgpu_measure(handle_.get(), count, shot_seed(), idx.data(), cnt.data(), cap, &nu,
+                               &failed));
+            for (size_t i = 0; i < nu; ++i)
+                bins[ProductState::binary_basis(idx[i], num_qubits_)] += (size_t)cnt[i];
+            if (!disable_warnings_)
+                for (uint64_t f = 0; f < failed; ++f)
+                    std::cerr << "\x1b[93m[Quantr Warning] The superposition failed to collapse to "
+                                 "a state during repeat measurements. This is likely due to the "
+                                 "use of Gate::Custom where the mapping is not unitary.\x1b[0m\n";
+        };
+        add(1);
+        if (progress_) std::cout << "Measured state # 1/" << shots << "\n";
+        bool stochastic = false;
+        for (const Gate& g : circuit_gates_) stochastic |= g.is_custom_gate();
+        std::optional<Program> last;
+        size_t pending = 0;
+        for (size_t s = 0; s + 1 < shots; ++s) {
+            if (!last || stochastic) {
+                Program p = lower(circuit_gates_, num_qubits_, progress_);
+                if (!last || p.mats != last->mats || p.none != last->none) {
+                    if (pending) add(pending);
+                    pending = 0;
+                    check(qgpu_set_zero(handle_.get()));
+                    apply(handle_.get(), p);
+                    last = std::move(p);
+                }
+            }
+            ++pending;
+            if (progress_)
+                std::cout << "Register reset to zero state\nMeasured state # " << s + 2 << "/"
+                          << shots << "\n";
+        }
+        if (pending) add(pending);
         return {true, std::move(bins)};
     }
     Measurement<SuperPosition> get_state() const {
@@ -440,46 +542,7 @@ class Circuit {
         if (reg)
             check(qgpu_upload(h.get(), reinterpret_cast<const double*>(reg->amplitudes.data()),
                               reg->amplitudes.size()));
-        // lowering: simulation.rs:37-56
-        std::vector<qgpu_op> ops;
-        std::vector<double> mats;
-        std::vector<uint8_t> none;
-        size_t counter = 0;
-        for (const Gate& g : gates_) {
-            if (g.kind == QGPU_GATE_ID) {
-                ++counter;
-                continue;
-            }
-            qgpu_op op{};
-            op.kind = g.kind;
-            op.target = (int32_t)(counter % num_qubits_);
-            op.n_controls = (int32_t)g.controls.size();
-            for (size_t m = 0; m < g.controls.size() && m < QGPU_MAX_OP_WIRES; ++m)
-                op.controls[m] = (int32_t)g.controls[m];
-            op.param = g.angle;
-            op.k = g.k;
-            if (g.is_custom_gate()) {  // simulation.rs:137-156, tabulated
-                const size_t kq = g.controls.size() + 1, d = (size_t)1 << kq;
-                op.mat_offset = (int64_t)mats.size();
-                op.none_offset = (int64_t)none.size();
-                for (size_t j = 0; j < d; ++j) {
-                    auto img = g.func(ProductState::binary_basis(j, kq));
-                    none.push_back(img ? 0 : 1);
-                    for (size_t l = 0; l < d; ++l) {
-                        Complex64 v = (img && l < img->amplitudes.size()) ? img->amplitudes[l] : 0.0;
-                        mats.push_back(v.real());
-                        mats.push_back(v.imag());
-                    }
-                }
-            }
-            if (progress_)
-                std::cout << "Applying gate " << g.kind << " on wire " << op.target << " # "
-                          << counter + 1 << "/" << gates_.size() << " \n";
-            ops.push_back(op);
-            ++counter;
-        }
-        check(qgpu_apply_program(h.get(), ops.data(), ops.size(), mats.data(), mats.size(),
-                                 none.data(), none.size()));
+        apply(h.get(), lower(gates_, num_qubits_, progress_));  // simulation.rs:37-56
         return SimulatedCircuit(gates_, num_qubits_, std::move(h), progress_);
     }
 };

@@ -290,26 +290,49 @@ class SimulatedCircuit:
         return Observable(Histogram(idx, cnt, self.num_qubits))
 
     def measure_all_without_cache(self, shots: int) -> Observable:  # simulated_circuit.rs:81-114
-        """Shot 1 uses the cached register; every later shot re-simulates from |0...0>."""
+        """Shot 1 uses the cached register; every later shot re-simulates from |0...0>.
+
+        Each later shot re-tabulates every `Custom` gate (its function is called again, so a
+        function that draws random Kraus branches gets a fresh draw per shot, as in quantr). A
+        run of consecutive shots whose tables come out identical yields the same register, so
+        it is simulated once and sampled with one `measure` call for the whole run; a circuit
+        without `Custom` gates is simulated once for shots 2..N."""
+        if shots < 1:
+            raise QuantrError("measure_all_without_cache needs at least one shot.")
         bins: dict = {}
 
-        def add(sim):
-            idx, cnt, failed = sim._handle.measure(1, rng.next_u64())
+        def add(count):
+            idx, cnt, failed = self._handle.measure(int(count), rng.next_u64())
             if failed and not self.disable_warnings:
-                print(_WARN_NONE, file=sys.stderr)
+                for _ in range(failed):
+                    print(_WARN_NONE, file=sys.stderr)
             for i, c in zip(idx, cnt):
                 key = ProductState.binary_basis(int(i), self.num_qubits)
                 bins[key] = bins.get(key, 0) + int(c)
 
-        add(self)
-        prog = lower(self.circuit_gates, self.num_qubits)
+        add(1)
+        if self.config_progress:
+            print(f"Measured state # 1/{shots}")
+        stochastic = any(g.is_custom_gate() for g in self.circuit_gates)
+        last_key, pending = None, 0
+        prog = None
         for s in range(shots - 1):
-            self._handle.set_zero()
-            self._handle.apply(prog.ops, prog.mats, prog.none)
-            self._state = None
-            add(self)
+            if prog is None or stochastic:
+                prog = lower(self.circuit_gates, self.num_qubits)
+            key = (prog.mats.tobytes(), prog.none.tobytes())
+            if key != last_key:
+                if pending:
+                    add(pending)
+                self._handle.set_zero()
+                self._handle.apply(prog.ops, prog.mats, prog.none)
+                self._state = None
+                last_key, pending = key, 0
+            pending += 1
             if self.config_progress:
+                print("Register reset to zero state")
                 print(f"Measured state # {s + 2}/{shots}")
+        if pending:
+            add(pending)
         return Observable(bins)
 
     def get_state(self) -> NonObservable:  # simulated_circuit.rs:158-160

@@ -371,10 +371,50 @@ struct PolRaw {
     static __device__ __forceinline__ S store(const R& r) { return r; }
 };
 
+// ---- resident float-pair layout ---------------------------------------------------------------
+// During a run of float-pair passes the register can stay in float-pair form: each 16-byte
+// amplitude slot holds (re_h, im_h | re_l, im_l) instead of (re, im) as doubles. Loads and stores
+// are then plain register moves (no split, no join on the FP64 pipe); k_ff_layout converts the
+// whole register once before the run and once after it.
+__device__ __forceinline__ ffp ffr_load(double2 a) {
+    ffp r;
+    r.h = (u64)__double_as_longlong(a.x);
+    r.l = (u64)__double_as_longlong(a.y);
+    return r;
+}
+__device__ __forceinline__ double2 ffr_store(const ffp& r) {
+    return make_double2(__longlong_as_double((long long)r.h), __longlong_as_double((long long)r.l));
+}
+
+struct PolFFR : PolFF {
+    static __device__ __forceinline__ R load(S a) { return ffr_load(a); }
+    static __device__ __forceinline__ S store(const R& r) { return ffr_store(r); }
+};
+
+// moves and +-1/+-i phases on the resident layout (a phase of i swaps and negates both halves)
+struct PolRawFFR {
+    using S = double2;
+    using R = ffp;
+    static __device__ __forceinline__ R load(S a) { return ffr_load(a); }
+    static __device__ __forceinline__ S store(const R& r) { return ffr_store(r); }
+};
+
+// to_pairs: complex128 -> resident float pairs; otherwise back (in place, one pass each)
+template <bool TO_PAIRS>
+__global__ void __launch_bounds__(256) k_ff_layout(double2* __restrict__ st, uint64_t dim) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += stride) {
+        const double2 a = st[i];
+        st[i] = TO_PAIRS ? ffr_store(to_ffp(a)) : from_ffp(ffr_load(a));
+    }
+}
+
 template <class P>
 struct IsArith { static constexpr bool value = true; };
 template <class T>
 struct IsArith<PolRaw<T>> { static constexpr bool value = false; };
+template <>
+struct IsArith<PolRawFFR> { static constexpr bool value = false; };
 
 // Applies step s to the 2^K amplitudes v of one tile (full indices base | off[j]).
 template <int K, int B, class P>
@@ -527,9 +567,27 @@ __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, co
 #pragma unroll
             for (int j = 0; j < T; ++j) v[u][j] = P::load(raw[u][j]);
         // step-major: each step's constants and dispatch are read once for all U groups
-        if constexpr (ONE == ST_DENSE && IsArith<P>::value) {
+        if constexpr (ONE == ST_DENSE && IsArith<P>::value && K == 1) {
 #pragma unroll
             for (int u = 0; u < U; ++u) P::dense(v[u][0], v[u][1], p.steps[0]);
+        } else if constexpr (ONE == ST_DENSE && IsArith<P>::value && K == 2) {
+            // every step an unconditional dense 2x2 on tile bit 0 or 1 (fused single-wire gates)
+            for (int s = 0; s < p.nsteps; ++s) {
+                const DevStep& sp = p.steps[s];
+                if (sp.lb == 0) {
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        P::dense(v[u][0], v[u][1], sp);
+                        P::dense(v[u][2], v[u][3], sp);
+                    }
+                } else {
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        P::dense(v[u][0], v[u][2], sp);
+                        P::dense(v[u][1], v[u][3], sp);
+                    }
+                }
+            }
         } else if constexpr (ONE == ST_REAL && IsArith<P>::value) {
 #pragma unroll
             for (int u = 0; u < U; ++u) P::real(v[u][0], v[u][1], p.steps[0]);
@@ -715,6 +773,8 @@ static int launch_xor(qgpu_handle* h, const XorPerm& xp) {
     return QGPU_OK;
 }
 
+static int env_int(const char* name, int dflt);
+
 template <int K, int U, class P>
 static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
     const uint64_t per_block = 256ull * U;
@@ -735,14 +795,22 @@ static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
             }
         }
     }
+    if constexpr (K == 2 && IsArith<P>::value) {
+        static const int straight = env_int("QGPU_K2_STRAIGHT", 1);
+        bool all_dense = straight != 0;
+        for (int i = 0; i < p.nsteps && all_dense; ++i)
+            all_dense = p.steps[i].type == ST_DENSE && p.steps[i].cm == 0;
+        if (all_dense) {
+            k_tile<K, U, P, ST_DENSE><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+            launched = true;
+        }
+    }
     if (!launched) k_tile<K, U, P><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
     QGPU_CHECK_LAUNCH("k_tile");
     h->launches++;
     h->h2d_bytes += sizeof(TileParams);
     return QGPU_OK;
 }
-
-static int env_int(const char* name, int dflt);
 
 template <class P>
 static int launch_tile_k(qgpu_handle* h, const TileParams& p) {
@@ -774,11 +842,37 @@ static int env_int(const char* name, int dflt) {
     return std::atoi(v);
 }
 
-static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, const float4* tab_ff,
-                       const double2* tab_f64, TileParams& tp);
+static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, bool resident,
+                       const float4* tab_ff, const double2* tab_f64, TileParams& tp);
+
+static int launch_ff_layout(qgpu_handle* h, bool to_pairs) {
+    uint64_t blocks = (h->dim + 255) / 256;
+    const uint64_t cap = (uint64_t)h->sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    double2* s = (double2*)cur_state(h);
+    if (to_pairs) k_ff_layout<true><<<(unsigned)blocks, 256, 0, h->stream>>>(s, h->dim);
+    else k_ff_layout<false><<<(unsigned)blocks, 256, 0, h->stream>>>(s, h->dim);
+    QGPU_CHECK_LAUNCH("k_ff_layout");
+    h->launches++;
+    return QGPU_OK;
+}
+
+// Whether a float-pair plan runs on the resident layout: it saves the split and join of every
+// arithmetic pass for two extra streaming passes, so it pays once the plan carries several
+// arithmetic passes. Custom blocks read complex128 and keep the plan on the plain layout.
+// QGPU_FF_RESIDENT=0/1 forces it off/on.
+static bool plan_resident(const qgpu_handle* h, const Plan& plan) {
+    if (policy_of(h) != POL_FF || !plan.customs.empty()) return false;
+    static const int force = env_int("QGPU_FF_RESIDENT", -1);
+    if (force >= 0) return force != 0;
+    int arith = 0;
+    for (const Pass& ps : plan.passes) arith += (ps.custom < 0 && !ps.xor_pass && ps.arith);
+    return arith >= 8;
+}
 
 static int run_plan(qgpu_handle* h, const Plan& plan) {
     const int pol = policy_of(h);
+    const bool resident = plan_resident(h, plan);
     // phase tables for every TABLE step of the plan, uploaded once
     const size_t nent = plan.table_f64.size() / 2;
     const float4* tab_ff = nullptr;
@@ -818,36 +912,45 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
     TileParams tp;
     std::vector<std::string> prof_names;
     std::vector<double> prof_bytes;
+    const size_t nlaunch = plan.passes.size() + (resident ? 2 : 0);
     if (h->profile) {
-        int st = prof_events(h, plan.passes.size());
+        int st = prof_events(h, nlaunch);
         if (st != QGPU_OK) return st;
     }
     static const char* pol_name[] = {"ff", "f64", "f32"};
     QGPU_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
-    for (size_t pi = 0; pi < plan.passes.size(); ++pi) {
-        const Pass& ps = plan.passes[pi];
+    const double full_bytes = 2.0 * (double)h->amp_bytes * (double)h->dim;
+    for (size_t li = 0; li < nlaunch; ++li) {
+        // launch li: [layout to pairs], passes..., [layout back]
+        const bool first_conv = resident && li == 0;
+        const bool last_conv = resident && li == nlaunch - 1;
+        const Pass* ps = (first_conv || last_conv) ? nullptr : &plan.passes[li - (resident ? 1 : 0)];
         if (h->profile) {
-            QGPU_CUDA(cudaEventRecord(h->events[2 * pi], h->stream));
-            if (ps.custom >= 0) {
+            QGPU_CUDA(cudaEventRecord(h->events[2 * li], h->stream));
+            if (!ps) {
+                prof_names.push_back("k_ff_layout");
+            } else if (ps->custom >= 0) {
                 prof_names.push_back("k_group");
-            } else if (ps.xor_pass) {
+            } else if (ps->xor_pass) {
                 prof_names.push_back("k_xor_perm");
             } else {
-                prof_names.push_back(std::string("k_tile<") + std::to_string(ps.nbits) + "," +
-                                     (ps.arith ? pol_name[pol] : "move") + ">");
+                prof_names.push_back(std::string("k_tile<") + std::to_string(ps->nbits) + "," +
+                                     (ps->arith ? (resident ? "ffr" : pol_name[pol]) : "move") + ">");
             }
-            prof_bytes.push_back(2.0 * (double)h->amp_bytes * (double)h->dim * ps.touched);
+            prof_bytes.push_back(full_bytes * (ps ? ps->touched : 1.0));
         }
         int st = QGPU_OK;
-        if (ps.custom >= 0) {
-            st = launch_group(h, gargs[ps.custom], (const uint8_t*)h->gates.ptr, lay[ps.custom]);
-        } else if (ps.xor_pass) {
-            st = launch_xor(h, ps.xp);
+        if (!ps) {
+            st = launch_ff_layout(h, first_conv);
+        } else if (ps->custom >= 0) {
+            st = launch_group(h, gargs[ps->custom], (const uint8_t*)h->gates.ptr, lay[ps->custom]);
+        } else if (ps->xor_pass) {
+            st = launch_xor(h, ps->xp);
         } else {
-            st = launch_pass(h, ps, pol, tab_ff, tab_f64, tp);
+            st = launch_pass(h, *ps, pol, resident, tab_ff, tab_f64, tp);
         }
         if (st != QGPU_OK) return st;
-        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * pi + 1], h->stream));
+        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * li + 1], h->stream));
     }
     int err = 0;
     QGPU_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -857,8 +960,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
     return st;
 }
 
-static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, const float4* tab_ff,
-                       const double2* tab_f64, TileParams& tp) {
+static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, bool resident,
+                       const float4* tab_ff, const double2* tab_f64, TileParams& tp) {
     {
         std::memset(&tp, 0, sizeof(tp));
         tp.nbits = ps.nbits;
@@ -873,7 +976,9 @@ static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, const float4* ta
         static const int prefetch = env_int("QGPU_PREFETCH", 0);
         tp.prefetch = prefetch;
         int st;
-        if (!ps.arith) {
+        if (resident) {
+            st = ps.arith ? launch_tile_k<PolFFR>(h, tp) : launch_tile_k<PolRawFFR>(h, tp);
+        } else if (!ps.arith) {
             st = (h->precision == QGPU_C64) ? launch_tile_k<PolRaw<float2>>(h, tp)
                                             : launch_tile_k<PolRaw<double2>>(h, tp);
         } else if (pol == POL_F32) {
@@ -890,7 +995,10 @@ static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, const float4* ta
 PlanOptions plan_options_for(const qgpu_handle* h) {
     PlanOptions o;
     o.policy = policy_of(h);
-    if (o.policy == POL_FF) o.budget = h->batch_budget > 0 ? h->batch_budget : env_int("QGPU_FF_BUDGET", 140);
+    // Float-pair budget: 280 admits two fused dense 2x2 steps per 2-bit pass. On the resident
+    // layout the 30-qubit brickwork+QFT step measured 2549 ms at 280 against 3625 ms at 140
+    // (one dense step per pass) on GB300.
+    if (o.policy == POL_FF) o.budget = h->batch_budget > 0 ? h->batch_budget : env_int("QGPU_FF_BUDGET", 280);
     else if (o.policy == POL_F32) o.budget = env_int("QGPU_F32_BUDGET", 48);
     else o.budget = env_int("QGPU_F64_BUDGET", 1 << 20);
     o.max_bits = std::max(2, std::min(env_int("QGPU_TILE_BITS", MAX_TILE_BITS), MAX_TILE_BITS));

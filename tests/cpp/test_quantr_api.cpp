@@ -150,6 +150,21 @@ int main() {
         std::printf("%s state_hash_map\n", ok ? "PASS" : "FAIL");
         if (!ok) ++failures;
     }
+    {  // simulated_circuit.rs:81-114 on a uniform 3-qubit register: every bin near shots/8
+        Circuit c = Circuit::new_(3);
+        c.add_repeating_gate(Gate::H(), {0, 1, 2});
+        auto sim = std::move(c).simulate();
+        auto bins = sim.measure_all_without_cache(4000).take();
+        size_t total = 0;
+        bool ok = bins.size() == 8;
+        for (auto& kv : bins) {
+            total += kv.second;
+            ok = ok && kv.second > 350 && kv.second < 650;
+        }
+        ok = ok && total == 4000;
+        std::printf("%s measure_all_without_cache\n", ok ? "PASS" : "FAIL");
+        if (!ok) ++failures;
+    }
     expect_error("catches_overlapping_control_nodes",
                  [] { Circuit::new_(3).add_gates({Gate::CNot(0), Gate::Id(), Gate::Id()}); });
     expect_error("control_node_greater_than_circuit_size",

@@ -339,3 +339,61 @@ def test_measure_all_without_cache_post_select():
     bins = sim.measure_all_without_cache(20).take()
     assert sum(bins.values()) == 20
     assert all(str(s)[1] == "0" for s in bins)
+
+
+def _launches_of_one_simulate(qc):
+    sim = qc.clone_and_simulate()
+    return sim.handle.launch_count()
+
+
+def test_measure_all_without_cache_deterministic_simulates_once():
+    """Identical tables for every shot: shots 2..N come from one re-simulation from |0...0>,
+    sampled in one call; the histogram follows |a|^2 of the |0...0> run."""
+    n = 10
+    qc = W.brickwork_qft_circuit(n, layers=3, seed=41)
+
+    def custom_x(ps):  # deterministic, unitary
+        out = ps.comp_basis() ^ 1
+        return SuperPosition.new_with_amplitudes([1.0 if i == out else 0.0 for i in range(2)])
+
+    qc.add_gate(Gate.Custom(custom_x, [], "X"), 1)
+    per_sim = _launches_of_one_simulate(qc)
+    sim = qc.clone_and_simulate()
+    sim.print_warnings(True)
+    probs = np.abs(sim.get_state().take().get_amplitudes()) ** 2
+    before = sim.handle.launch_count()
+    shots = 20000
+    bins = sim.measure_all_without_cache(shots).take()
+    used = sim.handle.launch_count() - before
+    assert sum(bins.values()) == shots
+    assert used <= 2 * per_sim + 64, (used, per_sim)
+    counts = np.zeros(2**n)
+    for s, c in bins.items():
+        counts[s.comp_basis()] += c
+    exp = probs / probs.sum() * shots
+    m = exp >= 5
+    chi2 = float((((counts - exp) ** 2)[m] / exp[m]).sum())
+    assert chi2 < m.sum() + 6 * math.sqrt(2 * m.sum()) + 60
+
+
+def test_measure_all_without_cache_stochastic_custom_redraws():
+    """A Custom function that draws a bit-flip per call (a mixed-state channel): each shot
+    re-tabulates it, so the outcome frequency follows the flip probability."""
+    draw = np.random.default_rng(7)
+    p = 0.3
+
+    def flip(ps):
+        bit = 1 if draw.random() < p else 0
+        out = ps.comp_basis() ^ bit
+        return SuperPosition.new_with_amplitudes([1.0 if i == out else 0.0 for i in range(2)])
+
+    qc = Circuit(1)
+    qc.add_gate(Gate.Custom(flip, [], "F"), 0)
+    sim = qc.simulate()
+    sim.print_warnings(True)
+    shots = 3000
+    bins = sim.measure_all_without_cache(shots).take()
+    ones = sum(c for s, c in bins.items() if str(s) == "1")
+    assert sum(bins.values()) == shots
+    sd = math.sqrt(shots * p * (1 - p))
+    assert abs(ones - shots * p) < 6 * sd + 1
