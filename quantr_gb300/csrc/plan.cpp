@@ -196,12 +196,12 @@ namespace {
 
 // A gate reduced to "controlled 2x2 on one bit" form, a swap of two bits, or a generic block.
 struct AGate {
-    enum Kind { ONE, SWAP, BLOCK } kind;
+    enum Kind { ONE, SWAP, BLOCK, PAIR } kind;
     int t = 0;          // target bit (full index)
     uint64_t cm = 0;    // control bits that must be 1
     cd u[2][2];         // u[out][in]
-    int a = 0, b = 0;   // SWAP bits
-    int block = -1;     // BLOCK: index into plan.customs
+    int a = 0, b = 0;   // SWAP bits; PAIR: hi, lo bits
+    int block = -1;     // BLOCK: index into plan.customs; PAIR: index into plan.pairs
     uint64_t support = 0;  // all bits the gate reads or writes
 };
 
@@ -323,6 +323,209 @@ int step_cost(const HStep& h, int policy) {
         case ST_TABLE: return ((ff ? 55 : 8) * s.nfields >> std::min(pc, 4)) + 4;
     }
     return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Pair fusion: gates confined to two wires become one 4x4 block when that costs less arithmetic
+// than applying them one by one. Measured in complex multiply-adds per amplitude: a 4x4 costs 4,
+// a dense 2x2 costs 2, a diagonal 1 (0.5 when one entry is 1), a permutation with unit phases 0,
+// each halved per control bit. A brickwork of dense single-wire layers joined by CNot bricks
+// fuses two layers of a wire pair and their CNot into one block (8 -> 4).
+// ---------------------------------------------------------------------------------------------
+double agate_macs(const AGate& g) {
+    const cd u00 = g.u[0][0], u01 = g.u[0][1], u10 = g.u[1][0], u11 = g.u[1][1];
+    double c;
+    if (is_zero(u01) && is_zero(u10)) {
+        const bool one0 = u00 == cd(1, 0), one1 = u11 == cd(1, 0);
+        const bool unit = unit_code(u00) >= 0 && unit_code(u11) >= 0;
+        c = unit ? 0.0 : ((one0 || one1) ? 0.5 : 1.0);
+    } else if (is_zero(u00) && is_zero(u11)) {
+        c = (unit_code(u01) >= 0 && unit_code(u10) >= 0) ? 0.0 : 1.0;
+    } else {
+        c = 2.0;
+    }
+    return std::ldexp(c, -popcount64(g.cm));
+}
+
+// 4x4 of a ONE gate whose support lies in {hi, lo}; local index l = 2 * bit(hi) + bit(lo).
+void pair_matrix(const AGate& g, int hi, int lo, cd out[4][4]) {
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) out[r][c] = 0.0;
+    auto full_of = [&](int l) -> uint64_t {
+        return ((l >> 1) & 1 ? 1ull << hi : 0ull) | ((l & 1) ? 1ull << lo : 0ull);
+    };
+    auto local_of = [&](uint64_t f) -> int {
+        return (int)(((f >> hi) & 1ull) << 1 | ((f >> lo) & 1ull));
+    };
+    for (int in = 0; in < 4; ++in) {
+        const uint64_t f = full_of(in);
+        if ((f & g.cm) != g.cm) {
+            out[in][in] = 1.0;
+            continue;
+        }
+        const int tb = (int)((f >> g.t) & 1ull);
+        for (int ob = 0; ob < 2; ++ob) {
+            const uint64_t fo = (f & ~(1ull << g.t)) | ((uint64_t)ob << g.t);
+            out[local_of(fo)][in] += g.u[ob][tb];
+        }
+    }
+}
+
+void set_term_raw(uint64_t* pk4, double c0, double c1) {
+    const float h0 = (float)c0, h1 = (float)c1;
+    const float l0 = (float)(c0 - (double)h0), l1 = (float)(c1 - (double)h1);
+    pk4[0] = pack2(h0, h1);
+    pk4[1] = pack2(l0, l1);
+    pk4[2] = pack2(-h0, -h1);
+    pk4[3] = pack2(-l0, -l1);
+}
+
+std::vector<AGate> fuse_pairs(const std::vector<AGate>& gates, int n, Plan* plan) {
+    struct Open {
+        uint64_t bits = 0;
+        std::vector<int> members;
+        bool live = false;
+        bool frozen = false;  // a standalone gate holding its wires: takes no further members
+    };
+    std::vector<Open> open;
+    std::vector<int> owner(n, -1);
+    std::vector<AGate> out;
+    out.reserve(gates.size());
+    auto close = [&](int oi) {
+        Open& o = open[oi];
+        for (int b = 0; b < n; ++b)
+            if ((o.bits >> b) & 1ull) owner[b] = -1;
+        o.live = false;
+        double macs = 0.0;
+        for (int gi : o.members) macs += agate_macs(gates[gi]);
+        if (o.frozen || popcount64(o.bits) != 2 || macs <= 4.0 + 1e-9) {
+            for (int gi : o.members) out.push_back(gates[gi]);
+            return;
+        }
+        PairBlock pb;
+        pb.hi = 63 - __builtin_clzll(o.bits);
+        pb.lo = __builtin_ctzll(o.bits);
+        cd acc[4][4];
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) acc[r][c] = r == c ? 1.0 : 0.0;
+        for (int gi : o.members) {  // acc <- G * acc, in circuit order
+            cd gm[4][4], nx[4][4];
+            pair_matrix(gates[gi], pb.hi, pb.lo, gm);
+            for (int r = 0; r < 4; ++r)
+                for (int c = 0; c < 4; ++c) {
+                    cd v = 0.0;
+                    for (int q = 0; q < 4; ++q) v += gm[r][q] * acc[q][c];
+                    nx[r][c] = v;
+                }
+            std::memcpy(acc, nx, sizeof(acc));
+        }
+        std::memcpy(pb.m, acc, sizeof(acc));
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) {
+                set_term_raw(pb.pk + 32 * r + 8 * c, acc[r][c].real(), acc[r][c].real());
+                set_term_raw(pb.pk + 32 * r + 8 * c + 4, -acc[r][c].imag(), acc[r][c].imag());
+            }
+        AGate a;
+        a.kind = AGate::PAIR;
+        a.a = pb.hi;
+        a.b = pb.lo;
+        a.block = (int)plan->pairs.size();
+        a.support = o.bits;
+        plan->pairs.push_back(pb);
+        out.push_back(a);
+    };
+    for (size_t gi = 0; gi < gates.size(); ++gi) {
+        const AGate& g = gates[gi];
+        const bool fusable = g.kind == AGate::ONE && popcount64(g.support) <= 2;
+        std::vector<int> os;
+        for (int b = 0; b < n; ++b)
+            if (((g.support >> b) & 1ull) && owner[b] >= 0 &&
+                std::find(os.begin(), os.end(), owner[b]) == os.end())
+                os.push_back(owner[b]);
+        {  // standalone gates end when a later gate reaches one of their wires: all of them go
+           // out together (they hold disjoint wires, so they commute) and stay one XOR run
+            bool hit = false;
+            std::vector<int> keep;
+            for (int oi : os) {
+                if (open[oi].frozen) hit = true;
+                else keep.push_back(oi);
+            }
+            if (hit)
+                for (size_t oi = 0; oi < open.size(); ++oi)
+                    if (open[oi].live && open[oi].frozen) close((int)oi);
+            os.swap(keep);
+        }
+        if (!fusable) {
+            for (int oi : os) close(oi);
+            out.push_back(g);
+            continue;
+        }
+        // A two-wire diagonal gate (CZ, CR, CRk) only joins a block on exactly its two wires;
+        // otherwise it goes out in place, so that diagonal runs keep their order and fold into
+        // phase tables instead of lingering in blocks that are never fused.
+        if (popcount64(g.support) == 2 && is_zero(g.u[0][1]) && is_zero(g.u[1][0]) &&
+            !(os.size() == 1 && open[os[0]].bits == g.support)) {
+            for (int oi : os) close(oi);
+            out.push_back(g);
+            continue;
+        }
+        uint64_t all = g.support;
+        for (int oi : os) all |= open[oi].bits;
+        if (popcount64(all) > 2) {  // blocks reaching outside this gate's wires end here
+            if (agate_macs(g) < 1.0) {
+                // A cheap two-wire gate (CNot, CZ, controlled phase) between blocks stays on its
+                // own: opening a block with it would capture the next gates of both wires, which
+                // pair better with the gates on their other neighbours (brickwork: the odd CNot
+                // layer stands alone, each even CNot joins the dense layers around it). It is
+                // emitted only when a later gate reaches its wires, so that standalone gates of
+                // one layer come out next to each other (and form one XOR run). Diagonal gates
+                // go out at once instead: they keep their order, and runs of them between two
+                // non-diagonal gates fold into phase tables (QFT rows).
+                for (int oi : os) close(oi);
+                if (is_zero(g.u[0][1]) && is_zero(g.u[1][0])) {
+                    out.push_back(g);
+                    continue;
+                }
+                open.emplace_back();
+                Open& f = open.back();
+                f.live = f.frozen = true;
+                f.bits = g.support;
+                f.members.push_back((int)gi);
+                for (int b = 0; b < n; ++b)
+                    if ((f.bits >> b) & 1ull) owner[b] = (int)open.size() - 1;
+                continue;
+            }
+            std::vector<int> keep;
+            for (int oi : os) {
+                if (open[oi].bits & ~g.support) close(oi);
+                else keep.push_back(oi);
+            }
+            os.swap(keep);
+        }
+        int into;
+        if (os.empty()) {
+            open.emplace_back();
+            into = (int)open.size() - 1;
+            open[into].live = true;
+        } else {
+            into = os[0];
+            for (size_t q = 1; q < os.size(); ++q) {  // disjoint blocks commute: concatenate
+                Open& o = open[os[q]];
+                open[into].bits |= o.bits;
+                open[into].members.insert(open[into].members.end(), o.members.begin(),
+                                          o.members.end());
+                o.live = false;
+                o.members.clear();
+            }
+        }
+        open[into].bits |= g.support;
+        open[into].members.push_back((int)gi);
+        for (int b = 0; b < n; ++b)
+            if ((open[into].bits >> b) & 1ull) owner[b] = into;
+    }
+    for (size_t oi = 0; oi < open.size(); ++oi)
+        if (open[oi].live) close((int)oi);
+    return out;
 }
 
 // Steps for a controlled 2x2 u on bit t under control mask cm.
@@ -480,6 +683,7 @@ DevStep dense_step(cd u00, cd u01, cd u10, cd u11) {
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
                const uint8_t* none, size_t n_none, const PlanOptions& opt, Plan* plan) {
     plan->passes.clear();
+    plan->pairs.clear();
     plan->customs.clear();
     plan->table_ff.clear();
     plan->table_f64.clear();
@@ -563,10 +767,21 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
         if (k == 1 && opt.merge_1q) pending[a.t] = (int)gates.size() - 1;
     }
 
+    if (opt.pair_fusion) gates = fuse_pairs(gates, n, plan);
+
     // 2. AGates -> steps.
     std::vector<HStep> steps;
     std::vector<int> block_at;  // steps index -> custom block (or -1)
     for (const AGate& g : gates) {
+        if (g.kind == AGate::PAIR) {
+            HStep h;
+            h.s = blank_step(ST_DENSE4);
+            h.need[0] = g.a;
+            h.need[1] = g.b;
+            h.s.tab_off[0] = (uint32_t)g.block;
+            steps.push_back(h);
+            continue;
+        }
         if (g.kind == AGate::BLOCK) {
             HStep h;
             h.s = blank_step(0xFF);
@@ -746,6 +961,19 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
             }
         }
         const HStep& h = steps[i];
+        if (h.s.type == ST_DENSE4) {  // a pair block is a pass of its own (k_pair)
+            flush();
+            Pass p;
+            p.nbits = 2;
+            p.bits[0] = std::min(h.need[0], h.need[1]);
+            p.bits[1] = std::max(h.need[0], h.need[1]);
+            p.arith = true;
+            p.cost = 380;
+            p.touched = 1.0;
+            p.pair = (int)h.s.tab_off[0];
+            plan->passes.push_back(p);
+            continue;
+        }
         std::vector<int> bits = cur_bits;
         for (int q = 0; q < 2; ++q)
             if (h.need[q] >= 0 && std::find(bits.begin(), bits.end(), h.need[q]) == bits.end())

@@ -43,6 +43,7 @@ enum StepType : uint8_t {
     ST_PHASE = 4,  // v *= d where (index & cm) == cm (any bits; unit d uses no arithmetic)
     ST_DIAG = 5,   // v *= (index bit fb) ? d1 : d0, under (index & cm) == cm
     ST_TABLE = 6,  // v *= prod_f T_f[(index >> shift_f) & (2^width_f - 1)], under cm
+    ST_DENSE4 = 7,  // 4x4 complex on two bits (a fused pair block; always a pass of its own)
 };
 
 constexpr int MAX_TILE_BITS = 3;
@@ -93,10 +94,21 @@ struct Pass {
     double touched = 1.0;              // fraction of amplitudes the pass may change
     std::vector<DevStep> steps;
     int custom = -1;                   // >= 0: this pass is a Custom gate (group kernel)
+    int pair = -1;                     // >= 0: this pass is pair block `pair` (k_pair kernel)
+};
+
+// A 4x4 block over full-index bits hi > lo, local index l = 2 * bit(hi) + bit(lo).
+// pk: packed Dot2 terms of the float-pair kernel, output r / input c at pk[32r + 8c ..+7]
+// (terms (Re, Re) on x_c and (-Im, Im) on swap(x_c), 4 slots each as in DevStep::pk).
+struct PairBlock {
+    int hi = 0, lo = 0;
+    cd m[4][4];                        // m[out][in]
+    uint64_t pk[128];
 };
 
 struct Plan {
     std::vector<Pass> passes;
+    std::vector<PairBlock> pairs;      // fused pair blocks
     std::vector<LocalGate> customs;    // Custom gates, run by the group kernel
     std::vector<float> table_ff;       // TABLE entries as float pairs (4 floats each)
     std::vector<double> table_f64;     // TABLE entries as f64 (2 doubles each)
@@ -112,6 +124,7 @@ struct PlanOptions {
     bool merge_1q = true;              // multiply runs of single-wire gates into one matrix
     bool fuse_diagonal = true;         // fold diagonal runs into phase tables
     bool xor_runs = true;              // runs of >= 3 commuting controlled-X gates -> one pass
+    bool pair_fusion = false;          // fuse gates on two wires into 4x4 blocks where cheaper
 };
 
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,

@@ -409,6 +409,58 @@ __global__ void __launch_bounds__(256) k_ff_layout(double2* __restrict__ st, uin
     }
 }
 
+// ---- pair blocks: a 4x4 complex matrix on two bits (fused gates on a wire pair) -------------
+struct PairParams {
+    uint64_t ngroups;
+    int lo, hi;                // full-index bits, lo < hi; local index l = 2 * bit(hi) + bit(lo)
+    uint64_t pk[128];          // PairBlock::pk
+};
+
+// v[r] <- sum_c m[r][c] v[c]: one 8-term packed Dot2 per output (terms x_c and swap(x_c))
+__device__ __forceinline__ void ff_pair(ffp v[4], const u64* c) {
+    ffp sw[4], o[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        sw[q].h = pswap(v[q].h);
+        sw[q].l = pswap(v[q].l);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const u64* cr = c + 32 * r;
+        PDot2 d;
+        d.first(cr, v[0].h, v[0].l);
+        d.add(cr + 4, sw[0].h, sw[0].l);
+#pragma unroll
+        for (int q = 1; q < 4; ++q) {
+            d.add(cr + 8 * q, v[q].h, v[q].l);
+            d.add(cr + 8 * q + 4, sw[q].h, sw[q].l);
+        }
+        d.result(o[r].h, o[r].l);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = o[q];
+}
+
+template <class P>
+__global__ void __launch_bounds__(256) k_pair(typename P::S* __restrict__ st,
+                                              const __grid_constant__ PairParams p) {
+    const uint64_t olo = 1ull << p.lo, ohi = 1ull << p.hi;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < p.ngroups; g += stride) {
+        const uint64_t b = insert_zero(insert_zero(g, p.lo), p.hi);
+        const uint64_t idx[4] = {b, b | olo, b | ohi, b | olo | ohi};
+        typename P::S raw[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) raw[j] = st[idx[j]];
+        ffp v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = P::load(raw[j]);
+        ff_pair(v, p.pk);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) st[idx[j]] = P::store(v[j]);
+    }
+}
+
 template <class P>
 struct IsArith { static constexpr bool value = true; };
 template <class T>
@@ -826,7 +878,10 @@ static int launch_tile_k(qgpu_handle* h, const TileParams& p) {
         case 1:
             if (use_pipe && h->n_qubits >= 13) return launch_tile1_pipe<P>(h, p);
             return k1_groups == 4 ? launch_tile_t<1, 4, P>(h, p) : launch_tile_t<1, 2, P>(h, p);
-        case 2: return launch_tile_t<2, 1, P>(h, p);
+        case 2: {
+            static const int k2_groups = env_int("QGPU_K2_GROUPS", 1);  // tuning knob: 1 or 2
+            return k2_groups == 2 ? launch_tile_t<2, 2, P>(h, p) : launch_tile_t<2, 1, P>(h, p);
+        }
         default: return launch_tile_t<3, 1, P>(h, p);
     }
 }
@@ -854,6 +909,25 @@ static int launch_ff_layout(qgpu_handle* h, bool to_pairs) {
     else k_ff_layout<false><<<(unsigned)blocks, 256, 0, h->stream>>>(s, h->dim);
     QGPU_CHECK_LAUNCH("k_ff_layout");
     h->launches++;
+    return QGPU_OK;
+}
+
+static int launch_pair(qgpu_handle* h, const PairBlock& pb, bool resident) {
+    PairParams p;
+    p.ngroups = h->dim >> 2;
+    p.lo = pb.lo;
+    p.hi = pb.hi;
+    std::memcpy(p.pk, pb.pk, sizeof(p.pk));
+    uint64_t blocks = (p.ngroups + 255) / 256;
+    const uint64_t cap = (uint64_t)h->sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    double2* s = (double2*)cur_state(h);
+    if (resident) k_pair<PolFFR><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+    else k_pair<PolFF><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+    QGPU_CHECK_LAUNCH("k_pair");
+    h->launches++;
+    h->h2d_bytes += sizeof(PairParams);
     return QGPU_OK;
 }
 
@@ -929,6 +1003,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
             QGPU_CUDA(cudaEventRecord(h->events[2 * li], h->stream));
             if (!ps) {
                 prof_names.push_back("k_ff_layout");
+            } else if (ps->pair >= 0) {
+                prof_names.push_back(resident ? "k_pair<ffr>" : "k_pair<ff>");
             } else if (ps->custom >= 0) {
                 prof_names.push_back("k_group");
             } else if (ps->xor_pass) {
@@ -942,6 +1018,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         int st = QGPU_OK;
         if (!ps) {
             st = launch_ff_layout(h, first_conv);
+        } else if (ps->pair >= 0) {
+            st = launch_pair(h, plan.pairs[ps->pair], resident);
         } else if (ps->custom >= 0) {
             st = launch_group(h, gargs[ps->custom], (const uint8_t*)h->gates.ptr, lay[ps->custom]);
         } else if (ps->xor_pass) {
@@ -1005,6 +1083,8 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     // float-pair arithmetic on 8 amplitudes per thread needs ~120 registers (2 CTAs per SM):
     // keep arithmetic passes at 2 tile bits
     o.max_arith_bits = o.policy == POL_FF ? env_int("QGPU_ARITH_TILE_BITS", 2) : MAX_TILE_BITS;
+    // 4x4 pair blocks (k_pair) for the float-pair policy; QGPU_PAIR_FUSION=0 turns them off
+    o.pair_fusion = o.policy == POL_FF && env_int("QGPU_PAIR_FUSION", 1) != 0;
     return o;
 }
 

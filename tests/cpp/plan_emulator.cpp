@@ -1,0 +1,219 @@
+// Host-side executor of the fused pass plan (quantr_gb300/csrc/plan.cpp) in complex128, so the
+// planner's merging, pair fusion, table folding, XOR runs and pass grouping can be checked
+// against the oracle on a machine without a GPU. Steps are applied with their f64 entries
+// (DevStep::d) in the order and on the amplitudes the tile kernels use.
+//
+// usage: plan_emulator n ops.bin mats.bin none.bin out.bin [pair_fusion budget max_arith_bits
+//                                                          plan_only]
+//   ops.bin: qgpu_op records; mats.bin: f64; none.bin: u8; out.bin receives 2^n complex128.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iterator>
+#include <string>
+#include <vector>
+
+#include "../../quantr_gb300/csrc/plan.h"
+
+namespace qgpu {
+int fail(int code, const std::string& msg) {
+    std::fprintf(stderr, "plan error: %s\n", msg.c_str());
+    return code;
+}
+}  // namespace qgpu
+
+using qgpu::cd;
+
+template <class T>
+static std::vector<T> read_all(const char* path) {
+    std::ifstream f(path, std::ios::binary);
+    std::vector<char> bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    std::vector<T> out(bytes.size() / sizeof(T));
+    if (!out.empty()) std::memcpy(out.data(), bytes.data(), out.size() * sizeof(T));
+    return out;
+}
+
+static uint64_t insert_zero(uint64_t x, int pos) {
+    const uint64_t low = x & ((1ull << pos) - 1ull);
+    return low | ((x >> pos) << (pos + 1));
+}
+
+static cd unit(int code) {
+    static const cd u[4] = {cd(1, 0), cd(0, 1), cd(-1, 0), cd(0, -1)};
+    return u[code & 3];
+}
+
+static cd entry(const qgpu::DevStep& s, int slot) { return cd(s.d[2 * slot], s.d[2 * slot + 1]); }
+
+static void apply_step(const qgpu::DevStep& s, const qgpu::Pass& p, const qgpu::Plan& plan,
+                       std::vector<cd>& v, uint64_t base, const std::vector<uint64_t>& off) {
+    const int T = (int)v.size();
+    auto pairs = [&](int lb, auto&& fn) {
+        for (int j = 0; j < T; ++j) {
+            if ((j >> lb) & 1) continue;
+            const int j1 = j | (1 << lb);
+            if (s.cm && ((base | off[j]) & s.cm) != s.cm) continue;
+            fn(j, j1);
+        }
+    };
+    switch (s.type) {
+        case qgpu::ST_DENSE:
+            pairs(s.lb, [&](int j, int j1) {
+                const cd a = v[j], b = v[j1];
+                v[j] = entry(s, 0) * a + entry(s, 1) * b;
+                v[j1] = entry(s, 2) * a + entry(s, 3) * b;
+            });
+            break;
+        case qgpu::ST_REAL:
+            pairs(s.lb, [&](int j, int j1) {
+                const cd a = v[j], b = v[j1];
+                v[j] = s.d[0] * a + s.d[2] * b;
+                v[j1] = s.d[4] * a + s.d[6] * b;
+            });
+            break;
+        case qgpu::ST_PERM:
+            pairs(s.lb, [&](int j, int j1) {
+                cd a = v[j], b = v[j1];
+                if (s.anti) std::swap(a, b);
+                v[j] = a * unit(s.u0);
+                v[j1] = b * unit(s.u1);
+            });
+            break;
+        case qgpu::ST_SWAP: {
+            const int A = std::min(s.lb, s.lb2), B = std::max(s.lb, s.lb2);
+            for (int j = 0; j < T; ++j)
+                if (((j >> A) & 1) == 0 && ((j >> B) & 1) == 1) {
+                    const int j2 = (j | (1 << A)) & ~(1 << B);
+                    std::swap(v[j], v[j2]);
+                }
+            break;
+        }
+        case qgpu::ST_PHASE:
+            for (int j = 0; j < T; ++j)
+                if (((base | off[j]) & s.cm) == s.cm) v[j] *= s.unit ? unit(s.u0) : entry(s, 0);
+            break;
+        case qgpu::ST_DIAG:
+            for (int j = 0; j < T; ++j) {
+                const uint64_t idx = base | off[j];
+                if ((idx & s.cm) != s.cm) continue;
+                const int bit = (int)((idx >> s.fb) & 1ull);
+                v[j] *= s.unit ? unit(bit ? s.u1 : s.u0) : entry(s, bit);
+            }
+            break;
+        case qgpu::ST_TABLE:
+            for (int j = 0; j < T; ++j) {
+                const uint64_t idx = base | off[j];
+                if ((idx & s.cm) != s.cm) continue;
+                for (int f = 0; f < s.nfields; ++f) {
+                    const uint64_t y = (idx >> s.tab_shift[f]) & ((1ull << s.tab_width[f]) - 1ull);
+                    const size_t e = s.tab_off[f] + y;
+                    v[j] *= cd(plan.table_f64[2 * e], plan.table_f64[2 * e + 1]);
+                }
+            }
+            break;
+        default:
+            std::fprintf(stderr, "unknown step type %d\n", s.type);
+            std::exit(3);
+    }
+    (void)p;
+}
+
+int main(int argc, char** argv) {
+    if (argc < 6) {
+        std::fprintf(stderr, "usage: %s n ops mats none out [pair budget arith_bits]\n", argv[0]);
+        return 2;
+    }
+    const int n = std::atoi(argv[1]);
+    auto ops = read_all<qgpu_op>(argv[2]);
+    auto mats = read_all<double>(argv[3]);
+    auto none = read_all<uint8_t>(argv[4]);
+    qgpu::PlanOptions opt;
+    opt.policy = qgpu::POL_FF;
+    opt.pair_fusion = argc > 6 ? std::atoi(argv[6]) != 0 : true;
+    opt.budget = argc > 7 ? std::atoi(argv[7]) : 280;
+    opt.max_arith_bits = argc > 8 ? std::atoi(argv[8]) : 2;
+    qgpu::Plan plan;
+    if (qgpu::build_plan(ops.data(), ops.size(), n, mats.data(), mats.size(), none.data(),
+                         none.size(), opt, &plan) != QGPU_OK)
+        return 1;
+    if (argc > 9 && std::atoi(argv[9]) != 0) {  // plan only: report the pass counts
+        int counts[3] = {0, 0, 0};
+        for (const qgpu::Pass& p : plan.passes)
+            ++counts[p.pair >= 0 ? 0 : (p.xor_pass ? 2 : 1)];
+        std::printf("passes %zu pair %d tile %d xor %d\n", plan.passes.size(), counts[0], counts[1],
+                    counts[2]);
+        return 0;
+    }
+    const uint64_t dim = 1ull << n;
+    std::vector<cd> st(dim);
+    st[0] = 1.0;
+    int npair = 0, ntile = 0, nxor = 0;
+    for (const qgpu::Pass& p : plan.passes) {
+        if (p.custom >= 0) {
+            std::fprintf(stderr, "custom passes are not emulated\n");
+            return 4;
+        }
+        if (p.pair >= 0) {
+            ++npair;
+            const qgpu::PairBlock& pb = plan.pairs[p.pair];
+            for (uint64_t g = 0; g < (dim >> 2); ++g) {
+                const uint64_t b = insert_zero(insert_zero(g, pb.lo), pb.hi);
+                const uint64_t idx[4] = {b, b | (1ull << pb.lo), b | (1ull << pb.hi),
+                                         b | (1ull << pb.lo) | (1ull << pb.hi)};
+                cd x[4], y[4];
+                for (int j = 0; j < 4; ++j) x[j] = st[idx[j]];
+                for (int r = 0; r < 4; ++r) {
+                    y[r] = 0.0;
+                    for (int c = 0; c < 4; ++c) y[r] += pb.m[r][c] * x[c];
+                }
+                for (int j = 0; j < 4; ++j) st[idx[j]] = y[j];
+            }
+            continue;
+        }
+        if (p.xor_pass) {
+            ++nxor;
+            const qgpu::XorPerm& xp = p.xp;
+            for (uint64_t i = 0; i < dim; ++i) {
+                uint64_t f = 0;
+                for (int e = 0; e < xp.nterms; ++e) {
+                    if (xp.grouped[e] == 1) {
+                        const uint64_t c = i & xp.cm[e];
+                        f |= xp.shift[e] > 0 ? (c >> xp.shift[e]) : (c << -xp.shift[e]);
+                    } else if (xp.grouped[e] == 2) {
+                        if (__builtin_popcountll(i & xp.cm[e]) == 1) f |= xp.cm[e];
+                    } else if ((i & xp.cm[e]) == xp.cm[e]) {
+                        f |= xp.tbit[e];
+                    }
+                }
+                const uint64_t j = i ^ f;
+                if (j > i) std::swap(st[i], st[j]);
+            }
+            continue;
+        }
+        ++ntile;
+        const int K = p.nbits, T = 1 << K;
+        std::vector<uint64_t> off(T);
+        for (int j = 0; j < T; ++j) {
+            uint64_t o = 0;
+            for (int m = 0; m < K; ++m)
+                if ((j >> m) & 1) o |= 1ull << p.bits[m];
+            off[j] = o;
+        }
+        std::vector<cd> v(T);
+        for (uint64_t g = 0; g < (dim >> K); ++g) {
+            uint64_t b = g;
+            for (int m = 0; m < K; ++m) b = insert_zero(b, p.bits[m]);
+            for (int j = 0; j < T; ++j) v[j] = st[b | off[j]];
+            for (const qgpu::DevStep& s : p.steps) apply_step(s, p, plan, v, b, off);
+            for (int j = 0; j < T; ++j) st[b | off[j]] = v[j];
+        }
+    }
+    std::ofstream out(argv[5], std::ios::binary);
+    out.write(reinterpret_cast<const char*>(st.data()), (std::streamsize)(dim * sizeof(cd)));
+    std::printf("passes %zu pair %d tile %d xor %d\n", plan.passes.size(), npair, ntile, nxor);
+    return 0;
+}

@@ -1,0 +1,124 @@
+"""The fused-pass planner (quantr_gb300/csrc/plan.cpp) on the host: tests/cpp/plan_emulator.cpp
+executes the planned passes in complex128 and the result is compared with the oracle.
+
+Bar: max |a_plan - a_oracle| <= 1e-12 (the planner multiplies gate matrices together, so the
+result is not value-equal to gate-by-gate application; the float-pair kernels add their own
+rounding on top, checked by the GPU parity tests).
+"""
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from quantr_gb300 import workloads as W
+from quantr_gb300.program import ProgramBuilder
+
+ROOT = Path(__file__).resolve().parent.parent
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def emulator(tmp_path_factory):
+    exe = tmp_path_factory.mktemp("plan") / "plan_emulator"
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", str(ROOT / "include"),
+           str(ROOT / "tests" / "cpp" / "plan_emulator.cpp"),
+           str(ROOT / "quantr_gb300" / "csrc" / "plan.cpp"), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def run_plan(emulator, prog, tmp_path, pair=1, budget=280, arith_bits=2):
+    f = {k: tmp_path / f"{k}.bin" for k in ("ops", "mats", "none", "out")}
+    np.ascontiguousarray(prog.ops).tofile(f["ops"])
+    np.ascontiguousarray(prog.mats, dtype=np.float64).tofile(f["mats"])
+    np.ascontiguousarray(prog.none, dtype=np.uint8).tofile(f["none"])
+    r = subprocess.run([str(emulator), str(prog.n), str(f["ops"]), str(f["mats"]), str(f["none"]),
+                        str(f["out"]), str(pair), str(budget), str(arith_bits)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    counts = dict(zip(r.stdout.split()[::2], map(int, r.stdout.split()[1::2])))
+    return np.fromfile(f["out"], dtype=np.complex128), counts
+
+
+@pytest.mark.parametrize("pair", [0, 1])
+@pytest.mark.parametrize("budget", [140, 280])
+@pytest.mark.parametrize("n", [6, 11])
+def test_brickwork_qft_plan(emulator, oracle, tmp_path, n, budget, pair):
+    prog = W.brickwork_qft(n=n, layers=20, seed=2)
+    out, counts = run_plan(emulator, prog, tmp_path, pair, budget)
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    assert np.max(np.abs(out - ref)) <= TOL
+    if pair:
+        # two layers of a wire pair and their CNot per block
+        assert counts["pair"] >= 10 * (n // 2) - n
+
+
+@pytest.mark.parametrize("seed", [1, 11, 12])
+def test_random_columns_plan(emulator, oracle, tmp_path, seed):
+    prog = W.random_columns(n=9, columns=40, seed=seed)
+    for pair in (0, 1):
+        out, _ = run_plan(emulator, prog, tmp_path, pair)
+        ref = oracle.simulate(prog, engine=oracle.DENSE)
+        assert np.max(np.abs(out - ref)) <= TOL
+
+
+def test_every_gate_plan(emulator, oracle, tmp_path):
+    """Each gate kind on each wire with controls above and below (no Custom)."""
+    n = 6
+    b = ProgramBuilder(n)
+    for t in range(n):
+        b.add("H", t)
+    for t in range(n):
+        for name in ("H", "X", "Y", "Z", "S", "Sdag", "T", "Tdag", "X90", "Y90", "MX90", "MY90"):
+            b.add(name, t)
+        for name in ("Rx", "Ry", "Rz", "Phase"):
+            b.add(name, t, (), param=0.3 + t)
+        for c in range(n):
+            if c == t:
+                continue
+            b.add("CNot", t, (c,))
+            b.add("Ry", c, (), param=0.1 * c + 0.2)
+            b.add("CY", t, (c,))
+            b.add("CZ", t, (c,))
+            b.add("Swap", t, (c,))
+            b.add("CR", t, (c,), param=0.7 * c - t)
+            b.add("CRk", t, (c,), k=1 + (c + t) % 5)
+            c2 = (c + 1 + t) % n
+            if c2 not in (c, t):
+                b.add("Toffoli", t, (c, c2))
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    for pair in (0, 1):
+        for arith_bits in (2, 3):
+            out, _ = run_plan(emulator, prog, tmp_path, pair, 280, arith_bits)
+            assert np.max(np.abs(out - ref)) <= TOL
+
+
+def test_pair_blocks_interleaved_wires(emulator, oracle, tmp_path):
+    """Blocks that must close when a gate reaches a third wire, merge when two single-wire
+    blocks meet, and stay open across gates on other wires."""
+    n = 7
+    rng = np.random.default_rng(4)
+    b = ProgramBuilder(n)
+    for _ in range(6):
+        for w in range(n):
+            b.add("Rx", w, (), param=float(rng.uniform(0, 6.3)))
+            b.add("Rz", w, (), param=float(rng.uniform(0, 6.3)))
+        b.add("CNot", 1, (0,))
+        b.add("Ry", 0, (), param=float(rng.uniform(0, 6.3)))  # second layer on the 0-1 pair
+        b.add("Ry", 1, (), param=float(rng.uniform(0, 6.3)))
+        b.add("CZ", 3, (2,))
+        b.add("CNot", 2, (1,))      # reaches across two open blocks
+        b.add("Ry", 4, (), param=0.4)
+        b.add("CNot", 5, (4,))
+        b.add("CNot", 4, (5,))
+        b.add("Toffoli", 6, (0, 5))  # not fusable: closes blocks on 0 and 5
+        b.add("CRk", 3, (6,), k=3)
+        b.add("Swap", 2, (5,))
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    out, counts = run_plan(emulator, prog, tmp_path, 1)
+    assert counts["pair"] > 0
+    assert np.max(np.abs(out - ref)) <= TOL
