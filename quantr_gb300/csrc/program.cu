@@ -441,23 +441,97 @@ __device__ __forceinline__ void ff_pair(ffp v[4], const u64* c) {
     for (int q = 0; q < 4; ++q) v[q] = o[q];
 }
 
-template <class P>
+// VARIANT 0: one quad per thread per iteration. 1: the next iteration's quad is loaded into
+// registers before the current one is computed (loads in flight during the arithmetic).
+// 2: two quads per thread per iteration (constants read once for both).
+template <class P, int VARIANT>
 __global__ void __launch_bounds__(256) k_pair(typename P::S* __restrict__ st,
                                               const __grid_constant__ PairParams p) {
+    using S = typename P::S;
     const uint64_t olo = 1ull << p.lo, ohi = 1ull << p.hi;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < p.ngroups; g += stride) {
+    auto quad = [&](uint64_t g, uint64_t idx[4]) {
         const uint64_t b = insert_zero(insert_zero(g, p.lo), p.hi);
-        const uint64_t idx[4] = {b, b | olo, b | ohi, b | olo | ohi};
-        typename P::S raw[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) raw[j] = st[idx[j]];
+        idx[0] = b;
+        idx[1] = b | olo;
+        idx[2] = b | ohi;
+        idx[3] = b | olo | ohi;
+    };
+    auto compute = [&](const S raw[4], const uint64_t idx[4]) {
         ffp v[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) v[j] = P::load(raw[j]);
         ff_pair(v, p.pk);
 #pragma unroll
         for (int j = 0; j < 4; ++j) st[idx[j]] = P::store(v[j]);
+    };
+    if constexpr (VARIANT == 2) {
+        const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * 2;
+        for (uint64_t g0 = blockIdx.x * (uint64_t)blockDim.x * 2 + threadIdx.x; g0 < p.ngroups;
+             g0 += stride) {
+            const uint64_t g1 = g0 + blockDim.x;
+            const bool has1 = g1 < p.ngroups;
+            uint64_t i0[4], i1[4];
+            quad(g0, i0);
+            quad(has1 ? g1 : g0, i1);
+            S r0[4], r1[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) r0[j] = st[i0[j]];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) r1[j] = st[i1[j]];
+            ffp v0[4], v1[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                v0[j] = P::load(r0[j]);
+                v1[j] = P::load(r1[j]);
+            }
+            ff_pair(v0, p.pk);
+            ff_pair(v1, p.pk);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) st[i0[j]] = P::store(v0[j]);
+            if (has1) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) st[i1[j]] = P::store(v1[j]);
+            }
+        }
+    } else if constexpr (VARIANT == 1) {
+        const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+        uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+        if (g >= p.ngroups) return;
+        uint64_t idx[4];
+        quad(g, idx);
+        S raw[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) raw[j] = st[idx[j]];
+        for (;;) {
+            const uint64_t gn = g + stride;
+            const bool more = gn < p.ngroups;
+            uint64_t nidx[4];
+            S nraw[4];
+            if (more) {
+                quad(gn, nidx);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) nraw[j] = st[nidx[j]];
+            }
+            compute(raw, idx);
+            if (!more) break;
+            g = gn;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                idx[j] = nidx[j];
+                raw[j] = nraw[j];
+            }
+        }
+    } else {
+        const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+        for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < p.ngroups;
+             g += stride) {
+            uint64_t idx[4];
+            quad(g, idx);
+            S raw[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) raw[j] = st[idx[j]];
+            compute(raw, idx);
+        }
     }
 }
 
@@ -923,8 +997,18 @@ static int launch_pair(qgpu_handle* h, const PairBlock& pb, bool resident) {
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     double2* s = (double2*)cur_state(h);
-    if (resident) k_pair<PolFFR><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
-    else k_pair<PolFF><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+    static const int variant = env_int("QGPU_PAIR_VARIANT", 0);  // tuning knob: 0, 1 or 2
+    if (variant == 2) {
+        blocks = std::max<uint64_t>(1, std::min<uint64_t>((p.ngroups + 511) / 512, cap));
+        if (resident) k_pair<PolFFR, 2><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+        else k_pair<PolFF, 2><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+    } else if (variant == 1) {
+        if (resident) k_pair<PolFFR, 1><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+        else k_pair<PolFF, 1><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+    } else {
+        if (resident) k_pair<PolFFR, 0><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+        else k_pair<PolFF, 0><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+    }
     QGPU_CHECK_LAUNCH("k_pair");
     h->launches++;
     h->h2d_bytes += sizeof(PairParams);
