@@ -212,7 +212,8 @@ def run_precision(args) -> None:
                                         "one_minus_fidelity": float(1.0 - fid),
                                         "norm_drift": float(nrm - 1.0)}
     peak = measured_peaks()["hbm_gbs"]
-    for n, prec, pname, block_layers in [(33, nat.QGPU_C64, "c64", 2), (32, nat.QGPU_C128, "c128", 1)]:
+    for n, prec, pname, block_layers in [(33, nat.QGPU_C64, "c64", args.precision_layers),
+                                         (32, nat.QGPU_C128, "c128", 1)]:
         res = {}
         for label, blocks, layers in [("tiles", 0, args.precision_layers), ("blocks", 1, block_layers)]:
             prog = W.brickwork_qft(n=n, layers=layers, seed=3, qft=False)

@@ -24,7 +24,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contra
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", str(ROOT / "include")]
 
-CU_SOURCES = ["state.cu", "program.cu", "measure.cu", "adjoint.cu", "blocks.cu", "batch.cu"]
+CU_SOURCES = ["state.cu", "program.cu", "measure.cu", "adjoint.cu", "blocks.cu", "blocks_tc.cu",
+              "batch.cu"]
 CXX_SOURCES = ["plan.cpp"]
 
 

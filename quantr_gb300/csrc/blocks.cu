@@ -12,7 +12,9 @@
 // and the f64 version far more so; the register-tile passes of program.cu apply the same gates
 // one by one at 8-16 FMAs per gate per amplitude.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "internal.cuh"
@@ -148,15 +150,12 @@ static int launch_block(qgpu_handle* h, const BlockArgs& a) {
     }
 }
 
-// Applies ops as fused dense blocks of at most `bq` wires / `mg` gates.
-int apply_blocks(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double* mats,
-                 size_t n_mats, const uint8_t* none, size_t n_none, int bq, int mg) {
-    std::vector<DenseBlock> blocks;
-    int st = build_blocks(ops, n_ops, h->n_qubits, mats, n_mats, none, n_none, bq, mg, &blocks);
-    if (st != QGPU_OK) return st;
-    for (const DenseBlock& b : blocks)
-        if (b.k > 6)
-            return fail(QGPU_ERR_UNSUPPORTED, "dense-block fusion: a gate acts on more than 6 wires");
+bool block_tc_supported(const qgpu_handle* h, const DenseBlock& b);               // blocks_tc.cu
+int apply_blocks_tc(qgpu_handle* h, const std::vector<DenseBlock>& blocks);       // blocks_tc.cu
+
+// Blocks on the CUDA cores (k_block), in order.
+static int apply_blocks_cc(qgpu_handle* h, const std::vector<DenseBlock>& blocks) {
+    int st = QGPU_OK;
     // all block matrices in one upload
     const size_t esz = h->precision == QGPU_C128 ? 16 : 8;
     std::vector<size_t> offs(blocks.size());
@@ -183,7 +182,18 @@ int apply_blocks(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double*
     st = h->tables.ensure(total ? total : 256);
     if (st != QGPU_OK) return st;
     QGPU_CUDA(copy_async(h, h->tables.ptr, host.data(), total, cudaMemcpyHostToDevice));
+    std::vector<std::string> names;
+    std::vector<double> bytes;
+    if (h->profile) {
+        st = prof_events(h, blocks.size());
+        if (st != QGPU_OK) return st;
+    }
     for (size_t i = 0; i < blocks.size(); ++i) {
+        if (h->profile) {
+            QGPU_CUDA(cudaEventRecord(h->events[2 * i], h->stream));
+            names.push_back("k_block<" + std::to_string(1 << blocks[i].k) + ">");
+            bytes.push_back(2.0 * (double)h->amp_bytes * (double)h->dim);
+        }
         BlockArgs a;
         std::memset(&a, 0, sizeof(a));
         a.k = blocks[i].k;
@@ -192,8 +202,39 @@ int apply_blocks(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double*
         a.M = (const uint8_t*)h->tables.ptr + offs[i];
         st = (h->precision == QGPU_C128) ? launch_block<double2>(h, a) : launch_block<float2>(h, a);
         if (st != QGPU_OK) return st;
+        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * i + 1], h->stream));
+    }
+    if (h->profile) {
+        st = prof_collect(h, names, bytes);
+        if (st != QGPU_OK) return st;
     }
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    return QGPU_OK;
+}
+
+// Applies ops as fused dense blocks of at most `bq` wires / `mg` gates: complex64 blocks of 3 to 6
+// wires on the tensor cores (k_block_tc; QGPU_BLOCK_TC=0 keeps them on the CUDA cores), the rest
+// with k_block, in circuit order.
+int apply_blocks(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double* mats,
+                 size_t n_mats, const uint8_t* none, size_t n_none, int bq, int mg) {
+    std::vector<DenseBlock> blocks;
+    int st = build_blocks(ops, n_ops, h->n_qubits, mats, n_mats, none, n_none, bq, mg, &blocks);
+    if (st != QGPU_OK) return st;
+    for (const DenseBlock& b : blocks)
+        if (b.k > 6)
+            return fail(QGPU_ERR_UNSUPPORTED, "dense-block fusion: a gate acts on more than 6 wires");
+    const char* env = std::getenv("QGPU_BLOCK_TC");
+    const bool use_tc = !(env && env[0] == '0');
+    size_t i = 0;
+    while (i < blocks.size()) {  // consecutive runs of one kind
+        const bool tc = use_tc && block_tc_supported(h, blocks[i]);
+        size_t j = i + 1;
+        while (j < blocks.size() && (use_tc && block_tc_supported(h, blocks[j])) == tc) ++j;
+        std::vector<DenseBlock> run(blocks.begin() + i, blocks.begin() + j);
+        st = tc ? apply_blocks_tc(h, run) : apply_blocks_cc(h, run);
+        if (st != QGPU_OK) return st;
+        i = j;
+    }
     return QGPU_OK;
 }
 

@@ -78,3 +78,31 @@ def test_precision_cross_check_26q():
         assert infid <= 1e-8, (blocks, infid)
         assert e <= 1e-5, (blocks, e)
         assert abs(n64 - 1.0) <= 1e-4, (blocks, n64)
+
+
+@pytest.mark.parametrize("n,bq", [(13, 6), (16, 6), (14, 5), (12, 4), (10, 3)])
+def test_c64_tensor_core_blocks(oracle, monkeypatch, n, bq):
+    """complex64 blocks of 3-6 wires run on the tensor cores (k_block_tc, BF16x3 split): same
+    bars as the CUDA-core blocks against the complex128 oracle, on circuits whose blocks sit on
+    the lowest, the highest and scattered index bits; the CUDA-core path (QGPU_BLOCK_TC=0) is
+    computed too and must differ in rounding (proof the tensor-core path ran)."""
+    rng = np.random.default_rng(100 + n + bq)
+    b = ProgramBuilder(n)
+    for layer in range(6):
+        for w in range(n):
+            b.add("Rx", w, (), param=float(rng.uniform(0, 6.3)))
+            b.add("Rz", w, (), param=float(rng.uniform(0, 6.3)))
+        for w in range(layer % 2, n - 1, 2):
+            b.add("CNot", w + 1, (w,))
+        b.add("CRk", 0, (n - 1,), k=3)
+        b.add("Toffoli", n // 2, (1, n - 2))
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    monkeypatch.setenv("QGPU_BLOCK_TC", "1")
+    tc, _ = run(prog, precision=nat.QGPU_C64, blocks=bq)
+    monkeypatch.setenv("QGPU_BLOCK_TC", "0")
+    cc, _ = run(prog, precision=nat.QGPU_C64, blocks=bq)
+    for a in (tc, cc):
+        e, infid = _cross(a, ref)
+        assert e <= 1e-5 and infid <= 1e-8, (e, infid)
+    assert not np.array_equal(tc, cc)
