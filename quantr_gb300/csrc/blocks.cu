@@ -7,10 +7,11 @@
 // consecutive threads read consecutive groups: coalesced whenever the low index bits are not
 // block bits), each thread accumulates a 4 x 4 register tile of outputs (4 matrix rows x 4
 // groups) over the 2^k inputs, then the results go back through shared memory to coalesced
-// stores. complex64 accumulates in f32 FMA; complex128 in f64 FMA. A dense 64 x 64 block costs
-// 256 real FMAs per amplitude, so on GB300 the f32 version is compute-bound (~3x the HBM time)
-// and the f64 version far more so; the register-tile passes of program.cu apply the same gates
-// one by one at 8-16 FMAs per gate per amplitude.
+// stores. complex64 accumulates in f32 FMA (or runs on the tensor cores, blocks_tc.cu);
+// complex128 uses float-pair Dot2 arithmetic in the fast mode (k_block_ff) and f64 FMA in
+// QGPU_MODE_F64. A dense 64 x 64 block costs 256 real multiply-adds per amplitude, so on GB300
+// these CUDA-core versions are compute-bound; the register-tile passes of program.cu apply the
+// same gates one by one at 8-16 multiply-adds per gate per amplitude.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -118,6 +119,128 @@ __global__ void __launch_bounds__(BLK_THREADS) k_block(T* __restrict__ st, const
     }
 }
 
+// complex128 blocks in float-pair arithmetic (QGPU_MODE_FAST): the matrix sits in shared memory
+// as float pairs (re_h, re_l, im_h, im_l), the tile's inputs are split once into packed pairs,
+// and every output is one packed Dot2 over its 2D terms (M[l][j] x_j and the swapped lanes).
+// A thread owns RL rows x 4 groups; the CTA covers BFF_GT groups.
+constexpr int BFF_GT = 32;
+
+template <int D>
+__global__ void __launch_bounds__(BLK_THREADS) k_block_ff(double2* __restrict__ st,
+                                                          const __grid_constant__ BlockArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* sM = reinterpret_cast<float4*>(smem);  // [D][D]
+    ffp* sA = reinterpret_cast<ffp*>(sM + D * D);   // [D][BFF_GT] inputs
+    double2* sO = reinterpret_cast<double2*>(sA);   // [D][BFF_GT] outputs (after the inputs)
+    const float4* gM = reinterpret_cast<const float4*>(a.M);
+    for (int t = threadIdx.x; t < D * D; t += BLK_THREADS) sM[t] = gM[t];
+    constexpr int RG = 4, TX = BFF_GT / RG, TY = BLK_THREADS / TX;
+    constexpr int RL = D / TY > 0 ? D / TY : 1;
+    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    const bool active = ty * RL < D;
+    const uint64_t ntiles = (a.ngroups + BFF_GT - 1) / BFF_GT;
+    __syncthreads();
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t g0 = tile * BFF_GT;
+        for (int t = threadIdx.x; t < D * BFF_GT; t += BLK_THREADS) {
+            const int j = t / BFF_GT, gl = t % BFF_GT;
+            const uint64_t g = g0 + gl;
+            if (g >= a.ngroups) continue;
+            uint64_t base = g;
+            for (int m = 0; m < a.k; ++m) base = insert_zero(base, a.bits[m]);
+            uint64_t off = 0;
+            for (int m = 0; m < a.k; ++m)
+                if ((j >> m) & 1) off |= 1ull << a.bits[m];
+            sA[j * BFF_GT + gl] = to_ffp(st[base | off]);
+        }
+        __syncthreads();
+        PDot2 acc[RL][RG];
+        if (active) {
+            for (int j = 0; j < D; ++j) {
+                u64 c[RL][8];
+#pragma unroll
+                for (int r = 0; r < RL; ++r) {
+                    const float4 m = sM[(ty * RL + r) * D + j];
+                    c[r][0] = p2(m.x, m.x);
+                    c[r][1] = p2(m.y, m.y);
+                    c[r][2] = p2(-m.x, -m.x);
+                    c[r][3] = p2(-m.y, -m.y);
+                    c[r][4] = p2(-m.z, m.z);
+                    c[r][5] = p2(-m.w, m.w);
+                    c[r][6] = p2(m.z, -m.z);
+                    c[r][7] = p2(m.w, -m.w);
+                }
+#pragma unroll
+                for (int q = 0; q < RG; ++q) {
+                    const ffp x = sA[j * BFF_GT + tx * RG + q];
+                    const u64 xsh = pswap(x.h), xsl = pswap(x.l);
+#pragma unroll
+                    for (int r = 0; r < RL; ++r) {
+                        if (j == 0) acc[r][q].first(c[r], x.h, x.l);
+                        else acc[r][q].add(c[r], x.h, x.l);
+                        acc[r][q].add(c[r] + 4, xsh, xsl);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (active) {
+#pragma unroll
+            for (int r = 0; r < RL; ++r)
+#pragma unroll
+                for (int q = 0; q < RG; ++q) {
+                    ffp o;
+                    acc[r][q].result(o.h, o.l);
+                    sO[(ty * RL + r) * BFF_GT + tx * RG + q] = from_ffp(o);
+                }
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < D * BFF_GT; t += BLK_THREADS) {
+            const int j = t / BFF_GT, gl = t % BFF_GT;
+            const uint64_t g = g0 + gl;
+            if (g >= a.ngroups) continue;
+            uint64_t base = g;
+            for (int m = 0; m < a.k; ++m) base = insert_zero(base, a.bits[m]);
+            uint64_t off = 0;
+            for (int m = 0; m < a.k; ++m)
+                if ((j >> m) & 1) off |= 1ull << a.bits[m];
+            st[base | off] = sO[j * BFF_GT + gl];
+        }
+        __syncthreads();
+    }
+}
+
+template <int D>
+static int launch_block_ff_t(qgpu_handle* h, const BlockArgs& a) {
+    const size_t smem = (size_t)(D * D + D * BFF_GT) * 16;
+    static bool attr = false;
+    if (!attr) {
+        QGPU_CUDA(cudaFuncSetAttribute(k_block_ff<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+        attr = true;
+    }
+    const uint64_t ntiles = (a.ngroups + BFF_GT - 1) / BFF_GT;
+    uint64_t blocks = std::min<uint64_t>(ntiles, (uint64_t)h->sm_count * 2);
+    if (blocks < 1) blocks = 1;
+    k_block_ff<D><<<(unsigned)blocks, BLK_THREADS, smem, h->stream>>>((double2*)cur_state(h), a);
+    QGPU_CHECK_LAUNCH("k_block_ff");
+    h->launches++;
+    h->h2d_bytes += sizeof(BlockArgs);
+    return QGPU_OK;
+}
+
+static int launch_block_ff(qgpu_handle* h, const BlockArgs& a) {
+    switch (a.k) {
+        case 1: return launch_block_ff_t<2>(h, a);
+        case 2: return launch_block_ff_t<4>(h, a);
+        case 3: return launch_block_ff_t<8>(h, a);
+        case 4: return launch_block_ff_t<16>(h, a);
+        case 5: return launch_block_ff_t<32>(h, a);
+        case 6: return launch_block_ff_t<64>(h, a);
+        default: return fail(QGPU_ERR_UNSUPPORTED, "dense blocks act on at most 6 wires");
+    }
+}
+
 template <class T, int D>
 static int launch_block_t(qgpu_handle* h, const BlockArgs& a) {
     const size_t smem = (size_t)(D * D + D * BLK_GT) * sizeof(T);
@@ -156,6 +279,8 @@ int apply_blocks_tc(qgpu_handle* h, const std::vector<DenseBlock>& blocks);     
 // Blocks on the CUDA cores (k_block), in order.
 static int apply_blocks_cc(qgpu_handle* h, const std::vector<DenseBlock>& blocks) {
     int st = QGPU_OK;
+    // complex128 in the fast mode: float-pair kernel (k_block_ff); QGPU_MODE_F64: f64 FMA
+    const bool ff = h->precision == QGPU_C128 && h->mode != QGPU_MODE_F64;
     // all block matrices in one upload
     const size_t esz = h->precision == QGPU_C128 ? 16 : 8;
     std::vector<size_t> offs(blocks.size());
@@ -170,7 +295,12 @@ static int apply_blocks_cc(qgpu_handle* h, const std::vector<DenseBlock>& blocks
         const size_t D2 = (size_t)1 << (2 * blocks[i].k);
         for (size_t e = 0; e < D2; ++e) {
             const cd v = blocks[i].M[e];
-            if (esz == 16) {
+            if (ff) {  // (re_h, re_l, im_h, im_l)
+                const float rh = (float)v.real(), ih = (float)v.imag();
+                const float4 q = make_float4(rh, (float)(v.real() - (double)rh), ih,
+                                             (float)(v.imag() - (double)ih));
+                std::memcpy(host.data() + offs[i] + e * 16, &q, 16);
+            } else if (esz == 16) {
                 double2 d = make_double2(v.real(), v.imag());
                 std::memcpy(host.data() + offs[i] + e * 16, &d, 16);
             } else {
@@ -191,7 +321,7 @@ static int apply_blocks_cc(qgpu_handle* h, const std::vector<DenseBlock>& blocks
     for (size_t i = 0; i < blocks.size(); ++i) {
         if (h->profile) {
             QGPU_CUDA(cudaEventRecord(h->events[2 * i], h->stream));
-            names.push_back("k_block<" + std::to_string(1 << blocks[i].k) + ">");
+            names.push_back((ff ? "k_block_ff<" : "k_block<") + std::to_string(1 << blocks[i].k) + ">");
             bytes.push_back(2.0 * (double)h->amp_bytes * (double)h->dim);
         }
         BlockArgs a;
@@ -200,7 +330,8 @@ static int apply_blocks_cc(qgpu_handle* h, const std::vector<DenseBlock>& blocks
         for (int m = 0; m < a.k; ++m) a.bits[m] = blocks[i].bits[m];
         a.ngroups = h->dim >> a.k;
         a.M = (const uint8_t*)h->tables.ptr + offs[i];
-        st = (h->precision == QGPU_C128) ? launch_block<double2>(h, a) : launch_block<float2>(h, a);
+        st = ff ? launch_block_ff(h, a)
+                : (h->precision == QGPU_C128) ? launch_block<double2>(h, a) : launch_block<float2>(h, a);
         if (st != QGPU_OK) return st;
         if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * i + 1], h->stream));
     }
