@@ -211,6 +211,9 @@ def run_precision(args) -> None:
         out["cross_check_26q"][name] = {"max_abs_err": float(np.max(np.abs(a - ref))),
                                         "one_minus_fidelity": float(1.0 - fid),
                                         "norm_drift": float(nrm - 1.0)}
+    if args.precision_cross_only:  # the 26-qubit cross-check alone (a small case for ncu)
+        print(json.dumps(out), flush=True)
+        return
     peak = measured_peaks()["hbm_gbs"]
     for n, prec, pname, block_layers in [(33, nat.QGPU_C64, "c64", args.precision_layers),
                                          (32, nat.QGPU_C128, "c128", 1)]:
@@ -468,6 +471,8 @@ def main() -> None:
                     help="headline: the 30q c128 line; precision: 33q c64 / 32q c128; batch: "
                          "4096 circuits of 10..24 qubits")
     ap.add_argument("--precision-layers", type=int, default=4)
+    ap.add_argument("--precision-cross-only", action="store_true",
+                    help="precision configuration: run only the 26-qubit cross-check")
     ap.add_argument("--batch-count", type=int, default=4096)
     args = ap.parse_args()
     if args.config == "precision":
