@@ -152,7 +152,7 @@ def cpu_reference_sample(n: int, budget_s: float, seed: int = 2) -> dict:
             "seconds": dt, "gates": gates}
 
 
-def adjoint_leg(reps: int = 5) -> dict:
+def adjoint_leg(reps: int = 5, shift: bool = True) -> dict:
     """Differentiation config: 20-qubit ansatz, 10 layers of Ry Rz + CNot ring (400 angles),
     H = sum a_i Z_i Z_i+1 + sum b_i X_i. Adjoint gradient vs parameter shift (+-pi/2, 800 plain
     simulations + energies) on the same GPU; host wall clock around the blocking calls."""
@@ -168,18 +168,19 @@ def adjoint_leg(reps: int = 5) -> dict:
     for _ in range(reps):
         e, g = GR.energy_and_gradient(h, prog, an.a, an.b)
     t_adj = (time.perf_counter() - t0) / reps
-    GR.energy(h, prog, an.a, an.b)
-    t0 = time.perf_counter()
-    ps = GR.parameter_shift(h, prog, an.a, an.b)
-    t_ps = time.perf_counter() - t0
-    h.close()
     nparam = int(np.isin(prog.ops["kind"], list(GR.ROTATIONS)).sum())
-    return {"workload": "20q ansatz, 10 layers Ry Rz + CNot ring, ZZ+X observable, c128",
-            "params": nparam, "energy": e, "adjoint_ms": 1e3 * t_adj,
-            "grads_per_s": nparam / t_adj, "param_shift_ms": 1e3 * t_ps,
-            "speedup_vs_param_shift": t_ps / t_adj,
-            "max_abs_diff_vs_param_shift": float(np.max(np.abs(g - ps))),
-            "timer": "host wall clock around blocking calls"}
+    out = {"workload": "20q ansatz, 10 layers Ry Rz + CNot ring, ZZ+X observable, c128",
+           "params": nparam, "energy": e, "adjoint_ms": 1e3 * t_adj,
+           "grads_per_s": nparam / t_adj, "timer": "host wall clock around blocking calls"}
+    if shift:
+        GR.energy(h, prog, an.a, an.b)
+        t0 = time.perf_counter()
+        ps = GR.parameter_shift(h, prog, an.a, an.b)
+        t_ps = time.perf_counter() - t0
+        out.update({"param_shift_ms": 1e3 * t_ps, "speedup_vs_param_shift": t_ps / t_adj,
+                    "max_abs_diff_vs_param_shift": float(np.max(np.abs(g - ps)))})
+    h.close()
+    return out
 
 
 def run_precision(args) -> None:
@@ -467,9 +468,13 @@ def main() -> None:
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--ref-n", type=int, default=14)
     ap.add_argument("--ref-budget", type=float, default=15.0)
-    ap.add_argument("--config", choices=["headline", "precision", "batch"], default="headline",
+    ap.add_argument("--config", choices=["headline", "precision", "batch", "adjoint"],
+                    default="headline",
                     help="headline: the 30q c128 line; precision: 33q c64 / 32q c128; batch: "
-                         "4096 circuits of 10..24 qubits")
+                         "4096 circuits of 10..24 qubits; adjoint: the differentiation leg alone")
+    ap.add_argument("--adjoint-reps", type=int, default=5)
+    ap.add_argument("--adjoint-no-shift", action="store_true",
+                    help="adjoint config: skip the parameter-shift comparison")
     ap.add_argument("--precision-layers", type=int, default=4)
     ap.add_argument("--precision-cross-only", action="store_true",
                     help="precision configuration: run only the 26-qubit cross-check")
@@ -477,6 +482,10 @@ def main() -> None:
     args = ap.parse_args()
     if args.config == "precision":
         run_precision(args)
+        return
+    if args.config == "adjoint":
+        print(json.dumps({"impl": "ours", "config": "adjoint",
+                          **adjoint_leg(args.adjoint_reps, not args.adjoint_no_shift)}), flush=True)
         return
     if args.config == "batch":
         run_batch_leg(args)

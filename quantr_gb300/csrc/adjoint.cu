@@ -6,11 +6,13 @@
 // For a rotation U_l = exp(-i theta P / 2) (quantr's Rx, Ry, Rz; P = X, Y, Z) the derivative is
 // dE/dtheta_l = 2 Re <lambda_l| dU_l |psi_{l-1}> = Im <lambda_l| P |phi_l>, read from the two
 // vectors before the gate is undone; Phase(theta) = exp(i theta / 2) I gives -Im <lambda|phi>.
-// Then phi <- U_l^dagger phi and lambda <- U_l^dagger lambda. One fused kernel (k_adj_1q) does
-// the gradient term and both updates of a single-wire gate in one pass; multi-wire gates are
-// undone with the fused gate passes of program.cu on each vector. All arithmetic here is f64.
+// Then phi <- U_l^dagger phi and lambda <- U_l^dagger lambda. In QGPU_MODE_FAST the runs of
+// single-wire gates go through k_adj_tile (all gates of a wire, or of two wires, per pass, float-
+// pair arithmetic); QGPU_MODE_F64 uses k_adj_1q, one gate per pass in f64. Multi-wire gates are
+// undone with the fused gate passes of program.cu on each vector.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -169,6 +171,173 @@ k_adj_1q_ff(double2* __restrict__ phi, double2* __restrict__ lam, uint64_t npair
     if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
 }
 
+// ---------------------------------------------------------------------------------------------
+// k_adj_tile<K>: a run of single-wire gates of the reverse sweep, on up to K wires, in one pass.
+// Gates on different wires commute, so the run is regrouped wire by wire (each wire's gates in
+// their reverse order); a thread holds the 2^K amplitudes of phi and lambda that differ in the
+// pass's K bits (as float pairs) and, step by step, adds the gate's gradient term and applies
+// V = U^dagger to both vectors, exactly as the one-gate sweep would. Gradient terms are packed
+// float-pair dot products (lane sums of l * x with per-lane signs), accumulated per step with the
+// Dot2 error terms and reduced per CTA in f64.
+// ---------------------------------------------------------------------------------------------
+constexpr int ADJ_TILE_STEPS = 4;   // gates per pass (registers: a Dot2 accumulator each)
+constexpr int ADJ_TILE_BITS = 2;    // wires per pass
+
+struct AdjTileStep {
+    int lb;      // tile bit
+    int gen;     // 0 none, 1 X, 2 Y, 3 Z, 4 global phase
+    int slot;    // gradient slot (row of partial), -1 for none
+    u64 pk[32];  // ST_DENSE packed constants of V
+};
+
+struct AdjTileParams {
+    uint64_t ngroups;
+    int nbits;
+    int bits[ADJ_TILE_BITS];
+    int nsteps;
+    int nb;  // CTAs (row length of partial)
+    AdjTileStep steps[ADJ_TILE_STEPS];
+};
+
+// acc += sum over lanes of (sr * l.re * x.re, si * l.im * x.im), all float pairs
+__device__ __forceinline__ void adj_term(PDot2& acc, bool& first, const ffp& l, const ffp& x,
+                                         float sr, float si) {
+    const u64 sg = p2(sr, si);
+    u64 c[4];
+    c[0] = pmul(l.h, sg);
+    c[1] = pmul(l.l, sg);
+    c[2] = pmul(c[0], p2(-1.f, -1.f));
+    c[3] = pmul(c[1], p2(-1.f, -1.f));
+    if (first) {
+        acc.first(c, x.h, x.l);
+        first = false;
+    } else {
+        acc.add(c, x.h, x.l);
+    }
+}
+
+template <int K, int B>
+__device__ __forceinline__ void adj_tile_step(ffp* f, ffp* l, const AdjTileStep& s, PDot2& acc,
+                                              bool& first) {
+    constexpr int T = 1 << K;
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        if ((j >> B) & 1) continue;
+        const int j1 = j | (1 << B);
+        if (s.gen) {
+            const ffp f0 = f[j], f1 = f[j1], l0 = l[j], l1 = l[j1];
+            ffp f0s, f1s;  // swapped lanes (im, re)
+            f0s.h = pswap(f0.h);
+            f0s.l = pswap(f0.l);
+            f1s.h = pswap(f1.h);
+            f1s.l = pswap(f1.l);
+            // Re(conj(l) f) = lanes(l * f) with (+, +); Im(conj(l) f) = lanes(l * swap(f)), (+, -)
+            switch (s.gen) {
+                case 1:  // X: Im(l0* f1) + Im(l1* f0)
+                    adj_term(acc, first, l0, f1s, 1.f, -1.f);
+                    adj_term(acc, first, l1, f0s, 1.f, -1.f);
+                    break;
+                case 2:  // Y: -Re(l0* f1) + Re(l1* f0)
+                    adj_term(acc, first, l0, f1, -1.f, -1.f);
+                    adj_term(acc, first, l1, f0, 1.f, 1.f);
+                    break;
+                case 3:  // Z: Im(l0* f0) - Im(l1* f1)
+                    adj_term(acc, first, l0, f0s, 1.f, -1.f);
+                    adj_term(acc, first, l1, f1s, -1.f, 1.f);
+                    break;
+                default:  // global phase: -(Im(l0* f0) + Im(l1* f1))
+                    adj_term(acc, first, l0, f0s, -1.f, 1.f);
+                    adj_term(acc, first, l1, f1s, -1.f, 1.f);
+                    break;
+            }
+        }
+        ff_dense(f[j], f[j1], s.pk);
+        ff_dense(l[j], l[j1], s.pk);
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(ADJ_THREADS)
+k_adj_tile(double2* __restrict__ phi, double2* __restrict__ lam,
+           const __grid_constant__ AdjTileParams p, double* __restrict__ partial) {
+    constexpr int T = 1 << K;
+    __shared__ double sh[ADJ_THREADS];
+    uint64_t off[T];
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        uint64_t o = 0;
+#pragma unroll
+        for (int m = 0; m < K; ++m)
+            if ((j >> m) & 1) o |= 1ull << p.bits[m];
+        off[j] = o;
+    }
+    PDot2 acc[ADJ_TILE_STEPS];
+    bool first[ADJ_TILE_STEPS];
+#pragma unroll
+    for (int s = 0; s < ADJ_TILE_STEPS; ++s) {
+        first[s] = true;
+        acc[s].s = 0;
+        acc[s].en = 0;
+    }
+    for (uint64_t g = blockIdx.x * (uint64_t)ADJ_THREADS + threadIdx.x; g < p.ngroups;
+         g += (uint64_t)gridDim.x * ADJ_THREADS) {
+        uint64_t b = g;
+#pragma unroll
+        for (int m = 0; m < K; ++m) b = insert_zero(b, p.bits[m]);
+        ffp f[T], l[T];
+#pragma unroll
+        for (int j = 0; j < T; ++j) {
+            f[j] = to_ffp(phi[b | off[j]]);
+            l[j] = to_ffp(lam[b | off[j]]);
+        }
+#pragma unroll
+        for (int s = 0; s < ADJ_TILE_STEPS; ++s) {
+            if (s >= p.nsteps) break;
+            const AdjTileStep& st = p.steps[s];
+            if (st.lb == 0) adj_tile_step<K, 0>(f, l, st, acc[s], first[s]);
+            if constexpr (K > 1) if (st.lb == 1) adj_tile_step<K, (K > 1 ? 1 : 0)>(f, l, st, acc[s], first[s]);
+            if constexpr (K > 2) if (st.lb == 2) adj_tile_step<K, (K > 2 ? 2 : 0)>(f, l, st, acc[s], first[s]);
+        }
+#pragma unroll
+        for (int j = 0; j < T; ++j) {
+            phi[b | off[j]] = from_ffp(f[j]);
+            lam[b | off[j]] = from_ffp(l[j]);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < ADJ_TILE_STEPS; ++s) {
+        if (s >= p.nsteps) break;
+        if (p.steps[s].slot < 0) continue;
+        double v = 0.0;
+        if (!first[s]) {
+            u64 h, lo;
+            acc[s].result(h, lo);
+            float h0, h1, l0, l1;
+            up2(h, h0, h1);
+            up2(lo, l0, l1);
+            v = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
+        }
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int w = ADJ_THREADS / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) partial[(size_t)p.steps[s].slot * p.nb + blockIdx.x] = sh[0];
+        __syncthreads();
+    }
+}
+
+template <int K>
+static int launch_adj_tile(qgpu_handle* h, double2* phi, double2* lam, const AdjTileParams& p,
+                           double* partial) {
+    k_adj_tile<K><<<p.nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, p, partial);
+    QGPU_CHECK_LAUNCH("k_adj_tile");
+    h->launches++;
+    h->h2d_bytes += sizeof(AdjTileParams);
+    return QGPU_OK;
+}
+
 // grads[g] = sum over blocks of partial[g * nb + b], for g in [0, ng)
 __global__ void k_sum_partials(const double* __restrict__ partial, int nb, int ng,
                                double* __restrict__ out) {
@@ -314,17 +483,98 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
         seg.clear();
         return s2;
     };
+    // QGPU_MODE_FAST: runs of single-wire gates go through k_adj_tile, up to 2 wires and 4 gates
+    // per pass; each wire keeps its gates in reverse order (gates on other wires commute).
+    // Wires per pass (tuning knob QGPU_ADJ_TILE_BITS: 1 or 2). One wire per pass measured faster
+    // on GB300 (20-qubit ansatz: 10.2 ms against 11.2 ms): the 2-wire kernel needs 162 registers,
+    // one CTA per SM, and is latency-bound.
+    static const int tile_bits = [] {
+        const char* e = std::getenv("QGPU_ADJ_TILE_BITS");
+        return (e && e[0] == '2') ? 2 : 1;
+    }();
+    std::vector<size_t> run;  // op indices of the current single-wire run, in reverse order
+    auto flush_run = [&]() -> int {
+        if (run.empty()) return QGPU_OK;
+        std::vector<int> wires;                  // bit of each wire, in first-seen order
+        std::vector<std::vector<size_t>> gates;  // per wire, its ops in reverse order
+        for (size_t gi : run) {
+            const int bit = h->n_qubits - 1 - ops[gi].target;
+            size_t w = std::find(wires.begin(), wires.end(), bit) - wires.begin();
+            if (w == wires.size()) {
+                wires.push_back(bit);
+                gates.emplace_back();
+            }
+            gates[w].push_back(gi);
+        }
+        run.clear();
+        AdjTileParams p;
+        std::vector<std::pair<int, size_t>> pend;  // (bit, op) of the pass being filled
+        std::vector<int> pbits;
+        auto launch = [&]() -> int {
+            if (pend.empty()) return QGPU_OK;
+            std::memset(&p, 0, sizeof(p));
+            std::sort(pbits.begin(), pbits.end());
+            p.nbits = (int)pbits.size();
+            for (int m = 0; m < p.nbits; ++m) p.bits[m] = pbits[m];
+            p.ngroups = h->dim >> p.nbits;
+            p.nsteps = (int)pend.size();
+            p.nb = nb;
+            for (size_t q = 0; q < pend.size(); ++q) {
+                const qgpu_op& op = ops[pend[q].second];
+                AdjTileStep& t = p.steps[q];
+                t.lb = (int)(std::find(pbits.begin(), pbits.end(), pend[q].first) - pbits.begin());
+                switch (op.kind) {
+                    case QGPU_GATE_RX: t.gen = 1; break;
+                    case QGPU_GATE_RY: t.gen = 2; break;
+                    case QGPU_GATE_RZ: t.gen = 3; break;
+                    case QGPU_GATE_PHASE: t.gen = 4; break;
+                    default: t.gen = 0; break;
+                }
+                t.slot = rot_slot[pend[q].second];
+                LocalGate lg;
+                int s3 = tabulate(inverse_op(op), h->n_qubits, nullptr, 0, nullptr, 0, &lg);
+                if (s3 != QGPU_OK) return s3;
+                // V[l][j] = M[j * 2 + l]
+                const DevStep ds = dense_step(lg.M[0], lg.M[2], lg.M[1], lg.M[3]);
+                std::memcpy(t.pk, ds.pk, sizeof(t.pk));
+            }
+            pend.clear();
+            pbits.clear();
+            return p.nbits == 1 ? launch_adj_tile<1>(h, phi, lam, p, partial)
+                                : launch_adj_tile<2>(h, phi, lam, p, partial);
+        };
+        for (size_t w = 0; w < wires.size(); ++w) {
+            for (size_t q = 0; q < gates[w].size(); ++q) {
+                const bool have = std::find(pbits.begin(), pbits.end(), wires[w]) != pbits.end();
+                if ((!have && (int)pbits.size() == tile_bits) || pend.size() == ADJ_TILE_STEPS) {
+                    int s2 = launch();
+                    if (s2 != QGPU_OK) return s2;
+                }
+                if (std::find(pbits.begin(), pbits.end(), wires[w]) == pbits.end())
+                    pbits.push_back(wires[w]);
+                pend.emplace_back(wires[w], gates[w][q]);
+            }
+        }
+        return launch();
+    };
+    const bool tiles = h->mode == QGPU_MODE_FAST;
     for (size_t gi = n_ops; gi-- > 0;) {
         const qgpu_op& op = ops[gi];
         if (op.kind == QGPU_GATE_ID) continue;
         int k = 1;
         op_arity(op, h->n_qubits, &k);
         if (k > 1) {
+            st = flush_run();
+            if (st != QGPU_OK) return st;
             seg.push_back(inverse_op(op));
             continue;
         }
         st = flush_seg();
         if (st != QGPU_OK) return st;
+        if (tiles) {
+            run.push_back(gi);
+            continue;
+        }
         LocalGate lg;
         st = tabulate(inverse_op(op), h->n_qubits, nullptr, 0, nullptr, 0, &lg);
         if (st != QGPU_OK) return st;
@@ -359,6 +609,8 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
         }
         h->launches++;
     }
+    st = flush_run();
+    if (st != QGPU_OK) return st;
     st = flush_seg();
     if (st != QGPU_OK) return st;
     if (nrot) {
