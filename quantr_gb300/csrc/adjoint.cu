@@ -22,6 +22,7 @@
 namespace qgpu {
 
 int apply_ops_on(qgpu_handle* h, void* buffer, const qgpu_op* ops, size_t n_ops);  // program.cu
+int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync);         // program.cu
 PlanOptions plan_options_for(const qgpu_handle* h);
 
 constexpr int ADJ_THREADS = 256;
@@ -476,10 +477,13 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
         if (is_rotation(ops[g].kind)) rot_slot[g] = (int)slot++;
     // reverse sweep
     std::vector<qgpu_op> seg;  // consecutive multi-wire gates, undone together
-    auto flush_seg = [&]() -> int {
+    auto flush_seg = [&]() -> int {  // one plan for both vectors, launches queued without a sync
         if (seg.empty()) return QGPU_OK;
-        int s2 = apply_ops_on(h, phi, seg.data(), seg.size());
-        if (s2 == QGPU_OK) s2 = apply_ops_on(h, lam, seg.data(), seg.size());
+        Plan plan;
+        int s2 = build_plan(seg.data(), seg.size(), h->n_qubits, nullptr, 0, nullptr, 0,
+                            plan_options_for(h), &plan);
+        if (s2 == QGPU_OK) s2 = run_plan_on(h, phi, plan, false);
+        if (s2 == QGPU_OK) s2 = run_plan_on(h, lam, plan, false);
         seg.clear();
         return s2;
     };

@@ -1028,7 +1028,7 @@ static bool plan_resident(const qgpu_handle* h, const Plan& plan) {
     return arith >= 8;
 }
 
-static int run_plan(qgpu_handle* h, const Plan& plan) {
+static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
     const int pol = policy_of(h);
     const bool resident = plan_resident(h, plan);
     // phase tables for every TABLE step of the plan, uploaded once
@@ -1114,6 +1114,7 @@ static int run_plan(qgpu_handle* h, const Plan& plan) {
         if (st != QGPU_OK) return st;
         if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * li + 1], h->stream));
     }
+    if (!sync && !h->profile) return QGPU_OK;  // the caller synchronises the stream later
     int err = 0;
     QGPU_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     int st = h->profile ? prof_collect(h, prof_names, prof_bytes) : QGPU_OK;
@@ -1177,13 +1178,21 @@ int apply_blocks(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double*
 
 // Runs non-Custom ops as fused passes on `buffer` (a state-sized device vector of the handle's
 // precision) instead of the register.
+int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync);
+
 int apply_ops_on(qgpu_handle* h, void* buffer, const qgpu_op* ops, size_t n_ops) {
     Plan plan;
     int st = build_plan(ops, n_ops, h->n_qubits, nullptr, 0, nullptr, 0, plan_options_for(h), &plan);
     if (st != QGPU_OK) return st;
+    return run_plan_on(h, buffer, plan, true);
+}
+
+// Runs an already built plan (no Custom gates) on `buffer`; with sync = false the launches are
+// only queued on the handle's stream (the plan's tables are copied before this returns).
+int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync) {
     void* saved = h->active;
     h->active = buffer;
-    st = run_plan(h, plan);
+    const int st = run_plan(h, plan, sync);
     h->active = saved;
     return st;
 }
