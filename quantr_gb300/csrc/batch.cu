@@ -8,11 +8,15 @@
 // qgpu_adjoint_grad on a handle per register size, with the float-pair fusion budget picked per
 // size bucket by timing the candidates on the bucket's first circuit.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.cuh"
@@ -333,22 +337,29 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
         cleanup();
 #undef BATCH_TRY
     }
-    // ---- large circuits: register-tile passes, one handle per size, tuned budget per bucket
-    std::map<int, qgpu_handle*> handles;
+    // ---- large circuits: register-tile passes. The fusion budget is tuned once per size (the
+    // forward pass timed per candidate); then W host threads, each with its own handles (and so
+    // its own stream), take circuits largest first from a shared counter, so that the launch and
+    // synchronisation overhead of medium circuits overlaps with other circuits' kernels.
+    if (large.empty()) return QGPU_OK;
+    std::stable_sort(large.begin(), large.end(), [&](size_t x, size_t y) {
+        return items[x].n_qubits > items[y].n_qubits;
+    });
     std::map<int, int> budget;
-    int st = QGPU_OK;
-    for (size_t i : large) {
-        const qgpu_batch_item& it = items[i];
-        qgpu_handle*& h = handles[it.n_qubits];
-        if (!h) {
+    {
+        std::map<int, qgpu_handle*> tune;
+        int st = QGPU_OK;
+        for (size_t i : large) {
+            const qgpu_batch_item& it = items[i];
+            if (budget.count(it.n_qubits)) continue;
+            qgpu_handle* h = nullptr;
             st = qgpu_create(it.n_qubits, QGPU_C128, &h);
             if (st != QGPU_OK) break;
-        }
-        const qgpu_op* po = ops + it.op_offset;
-        if (!budget.count(it.n_qubits)) {  // autotune: time the forward pass per candidate
+            tune[it.n_qubits] = h;
+            const qgpu_op* po = ops + it.op_offset;
             static const int cand[] = {100, 140, 200, 280};
             double best = 1e30;
-            int pick = 140;
+            int pick = 280;
             for (int b : cand) {
                 h->batch_budget = b;
                 qgpu_set_zero(h);
@@ -365,12 +376,50 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
             budget[it.n_qubits] = pick;
             if (tuned_budget) tuned_budget[it.n_qubits] = pick;
         }
-        h->batch_budget = budget[it.n_qubits];
-        qgpu_set_zero(h);
-        st = qgpu_adjoint_grad(h, po, (size_t)it.n_ops, nullptr, 0, nullptr, 0, obs + it.obs_offset,
-                               obs + it.obs_offset + it.n_qubits, &energies[i], grads + it.grad_offset);
-        if (st != QGPU_OK) break;
+        for (auto& kv : tune) qgpu_destroy(kv.second);
+        if (st != QGPU_OK) return st;
     }
-    for (auto& kv : handles) qgpu_destroy(kv.second);
-    return st;
+    const char* env = std::getenv("QGPU_BATCH_WORKERS");
+    const int workers = std::max(1, std::min(16, env ? std::atoi(env) : 4));
+    std::atomic<size_t> next{0};
+    std::atomic<int> first_err{QGPU_OK};
+    std::string err_msg;
+    std::mutex err_mu;
+    auto work = [&]() {
+        std::map<int, qgpu_handle*> handles;
+        for (;;) {
+            if (first_err.load() != QGPU_OK) break;
+            const size_t q = next.fetch_add(1);
+            if (q >= large.size()) break;
+            const size_t i = large[q];
+            const qgpu_batch_item& it = items[i];
+            qgpu_handle*& h = handles[it.n_qubits];
+            int st = QGPU_OK;
+            if (!h) st = qgpu_create(it.n_qubits, QGPU_C128, &h);
+            if (st == QGPU_OK) {
+                h->batch_budget = budget[it.n_qubits];
+                st = qgpu_set_zero(h);
+            }
+            if (st == QGPU_OK)
+                st = qgpu_adjoint_grad(h, ops + it.op_offset, (size_t)it.n_ops, nullptr, 0, nullptr, 0,
+                                       obs + it.obs_offset, obs + it.obs_offset + it.n_qubits,
+                                       &energies[i], grads + it.grad_offset);
+            if (st != QGPU_OK) {
+                int expect = QGPU_OK;
+                if (first_err.compare_exchange_strong(expect, st)) {
+                    std::lock_guard<std::mutex> lk(err_mu);
+                    err_msg = qgpu_last_error();
+                }
+                break;
+            }
+        }
+        for (auto& kv : handles)
+            if (kv.second) qgpu_destroy(kv.second);
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < workers; ++w) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    if (first_err.load() != QGPU_OK) return fail(first_err.load(), err_msg);
+    return QGPU_OK;
 }
