@@ -860,39 +860,166 @@ static int launch_tile1_pipe(qgpu_handle* h, const TileParams& p) {
 // smaller index of each pair swaps it, the other does nothing. Amplitudes no gate moves are not
 // touched.
 // ---------------------------------------------------------------------------------------------
-template <class S>
+__device__ __forceinline__ uint64_t xor_f(uint64_t i, const XorPerm& xp) {
+    uint64_t f = 0;
+    for (int e = 0; e < xp.nterms; ++e) {
+        if (xp.grouped[e] == 1) {
+            const uint64_t c = i & xp.cm[e];
+            f |= xp.shift[e] > 0 ? (c >> xp.shift[e]) : (c << -xp.shift[e]);
+        } else if (xp.grouped[e] == 2) {
+            if (__popcll(i & xp.cm[e]) == 1) f |= xp.cm[e];  // swap of two differing bits
+        } else if ((i & xp.cm[e]) == xp.cm[e]) {
+            f |= xp.tbit[e];
+        }
+    }
+    return f;
+}
+
+// U indices per thread (blockDim apart, so each of the U rounds is a coalesced warp access):
+// all loads of a thread are issued before its stores, U x the memory-level parallelism of one
+// index per thread (half the threads of a round have nothing to do: j < i).
+template <class S, int U>
 __global__ void __launch_bounds__(256) k_xor_perm(S* __restrict__ st, uint64_t dim,
                                                   const __grid_constant__ XorPerm xp) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += stride) {
-        uint64_t f = 0;
-        for (int e = 0; e < xp.nterms; ++e) {
-            if (xp.grouped[e] == 1) {
-                const uint64_t c = i & xp.cm[e];
-                f |= xp.shift[e] > 0 ? (c >> xp.shift[e]) : (c << -xp.shift[e]);
-            } else if (xp.grouped[e] == 2) {
-                if (__popcll(i & xp.cm[e]) == 1) f |= xp.cm[e];  // swap of two differing bits
-            } else if ((i & xp.cm[e]) == xp.cm[e]) {
-                f |= xp.tbit[e];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * U;
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x * U + threadIdx.x; i0 < dim; i0 += stride) {
+        uint64_t ii[U], jj[U];
+        bool act[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t i = i0 + (uint64_t)u * blockDim.x;
+            ii[u] = i;
+            jj[u] = i < dim ? (i ^ xor_f(i, xp)) : i;
+            act[u] = jj[u] > i;
+        }
+        S a[U], b[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (act[u]) {
+                a[u] = st[ii[u]];
+                b[u] = st[jj[u]];
             }
-        }
-        const uint64_t j = i ^ f;
-        if (j > i) {
-            const S a = st[i], b = st[j];
-            st[i] = b;
-            st[j] = a;
-        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (act[u]) {
+                st[ii[u]] = b[u];
+                st[jj[u]] = a[u];
+            }
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// k_bitperm: a run of disjoint swaps (a QFT's final bit reversal) permutes index bits: amplitude
+// x moves to pi(x), pi an involution on bit positions. Scattered one-by-one swaps of such a run
+// touch a different far-away DRAM page per lane; this kernel tiles instead. Tile bits B = the 5
+// lowest bits and their images (|B| <= 10, closed under pi); a tile = the 2^|B| amplitudes that
+// share all other bits (a base). pi maps tile(base) onto tile(pi(base)): a CTA owns both tiles of
+// a pair (or one tile that maps onto itself), stages them in shared memory with coalesced loads
+// (low bits fastest) and writes each destination tile with coalesced stores, in place.
+// ---------------------------------------------------------------------------------------------
+constexpr int BP_MAX_BITS = 10;
+
+struct BitPermArgs {
+    int nb;                    // |B|
+    int bits[BP_MAX_BITS];     // B, ascending: tile-local bit m <-> bits[m]
+    int perm[64];              // pi(b) for every index bit b
+    int n;
+    uint64_t nbases;           // 2^(n - nb)
+};
+
+template <class S>
+__global__ void __launch_bounds__(256) k_bitperm(S* __restrict__ st, const __grid_constant__ BitPermArgs p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int T = 1 << p.nb;
+    S* tA = reinterpret_cast<S*>(smem);
+    S* tB = tA + T;
+    uint64_t* offB = reinterpret_cast<uint64_t*>(tB + T);  // [T] spread of local index l over B
+    uint16_t* pl = reinterpret_cast<uint16_t*>(offB + T);   // [T] local index of pi(spread(l))
+    for (int l = threadIdx.x; l < T; l += blockDim.x) {
+        uint64_t o = 0;
+        int q = 0;
+        for (int m = 0; m < p.nb; ++m)
+            if ((l >> m) & 1) {
+                o |= 1ull << p.bits[m];
+                const int pb = p.perm[p.bits[m]];
+                for (int r = 0; r < p.nb; ++r)
+                    if (p.bits[r] == pb) q |= 1 << r;
+            }
+        offB[l] = o;
+        pl[l] = (uint16_t)q;
+    }
+    __syncthreads();
+    for (uint64_t bi = blockIdx.x; bi < p.nbases; bi += gridDim.x) {
+        uint64_t base = bi;
+        for (int m = 0; m < p.nb; ++m) base = insert_zero(base, p.bits[m]);
+        uint64_t pbase = 0;  // pi(base): non-B bits map to non-B bits
+        for (int b = 0; b < p.n; ++b)
+            if ((base >> b) & 1ull) pbase |= 1ull << p.perm[b];
+        if (pbase < base) continue;  // the partner tile's CTA moves this pair
+        const bool self = pbase == base;
+        for (int l = threadIdx.x; l < T; l += blockDim.x) {
+            tA[l] = st[base | offB[l]];
+            if (!self) tB[l] = st[pbase | offB[l]];
+        }
+        __syncthreads();
+        // destination d = base | spread(l) receives pi(d) = pbase | spread(pl[l])
+        for (int l = threadIdx.x; l < T; l += blockDim.x) {
+            st[base | offB[l]] = self ? tA[pl[l]] : tB[pl[l]];
+            if (!self) st[pbase | offB[l]] = tA[pl[l]];
+        }
+        __syncthreads();
+    }
+}
+
+// Whether an XOR pass is a run of swaps only; fills the bit permutation if so.
+static bool xor_as_bitperm(const qgpu_handle* h, const XorPerm& xp, BitPermArgs* a) {
+    if (xp.nterms == 0) return false;
+    std::memset(a, 0, sizeof(*a));
+    a->n = h->n_qubits;
+    for (int b = 0; b < 64; ++b) a->perm[b] = b;
+    for (int e = 0; e < xp.nterms; ++e) {
+        if (xp.grouped[e] != 2 || __builtin_popcountll(xp.cm[e]) != 2) return false;
+        const int b0 = __builtin_ctzll(xp.cm[e]), b1 = 63 - __builtin_clzll(xp.cm[e]);
+        if (a->perm[b0] != b0 || a->perm[b1] != b1) return false;  // swaps must be disjoint
+        a->perm[b0] = b1;
+        a->perm[b1] = b0;
+    }
+    uint64_t B = 0;
+    for (int b = 0; b < 5 && b < a->n; ++b) B |= (1ull << b) | (1ull << a->perm[b]);
+    a->nb = __builtin_popcountll(B);
+    if (a->nb > BP_MAX_BITS) return false;
+    for (int b = 0, m = 0; b < 64; ++b)
+        if ((B >> b) & 1ull) a->bits[m++] = b;
+    a->nbases = h->dim >> a->nb;
+    return true;
+}
+
+static int launch_bitperm(qgpu_handle* h, const BitPermArgs& a) {
+    const int T = 1 << a.nb;
+    const size_t smem = (size_t)T * (2 * h->amp_bytes + 8 + 2);
+    uint64_t blocks = std::min<uint64_t>(a.nbases, (uint64_t)h->sm_count * 8);
+    if (blocks < 1) blocks = 1;
+    if (h->precision == QGPU_C128)
+        k_bitperm<double2><<<(unsigned)blocks, 256, smem, h->stream>>>((double2*)cur_state(h), a);
+    else
+        k_bitperm<float2><<<(unsigned)blocks, 256, smem, h->stream>>>((float2*)cur_state(h), a);
+    QGPU_CHECK_LAUNCH("k_bitperm");
+    h->launches++;
+    h->h2d_bytes += sizeof(BitPermArgs);
+    return QGPU_OK;
+}
+
 static int launch_xor(qgpu_handle* h, const XorPerm& xp) {
-    uint64_t blocks = (h->dim + 255) / 256;
+    BitPermArgs bp;
+    if (xor_as_bitperm(h, xp, &bp)) return launch_bitperm(h, bp);
+    constexpr int U = 4;
+    uint64_t blocks = (h->dim + 256 * U - 1) / (256 * U);
     const uint64_t cap = (uint64_t)h->sm_count * 8;
     if (blocks > cap) blocks = cap;
     if (h->precision == QGPU_C128)
-        k_xor_perm<double2><<<(unsigned)blocks, 256, 0, h->stream>>>((double2*)cur_state(h), h->dim, xp);
+        k_xor_perm<double2, U><<<(unsigned)blocks, 256, 0, h->stream>>>((double2*)cur_state(h), h->dim, xp);
     else
-        k_xor_perm<float2><<<(unsigned)blocks, 256, 0, h->stream>>>((float2*)cur_state(h), h->dim, xp);
+        k_xor_perm<float2, U><<<(unsigned)blocks, 256, 0, h->stream>>>((float2*)cur_state(h), h->dim, xp);
     QGPU_CHECK_LAUNCH("k_xor_perm");
     h->launches++;
     h->h2d_bytes += sizeof(XorPerm);
@@ -1092,7 +1219,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
             } else if (ps->custom >= 0) {
                 prof_names.push_back("k_group");
             } else if (ps->xor_pass) {
-                prof_names.push_back("k_xor_perm");
+                BitPermArgs bp;
+                prof_names.push_back(xor_as_bitperm(h, ps->xp, &bp) ? "k_bitperm" : "k_xor_perm");
             } else {
                 prof_names.push_back(std::string("k_tile<") + std::to_string(ps->nbits) + "," +
                                      (ps->arith ? (resident ? "ffr" : pol_name[pol]) : "move") + ">");

@@ -158,6 +158,30 @@ def test_commuting_cx_runs(oracle, precision):
     assert np.max(np.abs(out - ref)) <= tol
 
 
+@pytest.mark.parametrize("precision", [nat.QGPU_C128, nat.QGPU_C64])
+@pytest.mark.parametrize("n,pairs", [
+    (12, [(i, 11 - i) for i in range(6)]),          # full bit reversal, even width
+    (13, [(i, 12 - i) for i in range(6)]),          # odd width: middle wire stays
+    (11, [(0, 5), (2, 9), (1, 10), (7, 3)]),        # scattered disjoint swaps
+    (9, [(8, 7), (0, 1)]),                          # two swaps, all in the lowest tile bits
+])
+def test_swap_runs_bit_permutation(oracle, precision, n, pairs):
+    """A run of disjoint Swap gates is one index-bit permutation (k_bitperm: tiles closed under
+    the permutation, moved in pairs); random register, every wire distinct."""
+    rng = np.random.default_rng(31 + n)
+    reg = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    reg /= np.linalg.norm(reg)
+    b = ProgramBuilder(n)
+    for a, c in pairs:
+        b.add("Swap", a, (c,))
+    prog = b.build()
+    if precision == nat.QGPU_C64:  # the register as the complex64 handle holds it
+        reg = reg.astype(np.complex64).astype(np.complex128)
+    ref = oracle.simulate(prog, reg, engine=oracle.DENSE)
+    out = run_gpu(prog, "fast", precision=precision, reg=reg)
+    assert np.array_equal(out, ref)  # a permutation moves values unchanged
+
+
 @pytest.mark.parametrize("mode", ["exact", "fast"])
 def test_custom_blocks_dense_nonunitary_and_wide(oracle, mode):
     """Custom gates: a dense 3-wire block with None entries, a non-unitary block, and the widest
