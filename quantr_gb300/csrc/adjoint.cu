@@ -339,6 +339,69 @@ static int launch_adj_tile(qgpu_handle* h, double2* phi, double2* lam, const Adj
     return QGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// k_linperm: a run of CNot / X / Swap gates maps basis index y to an affine function of y over
+// GF(2). The run is applied out of place as one gather, dst[y] = src[h(y)] with h the inverse
+// map (h(y) = d xor the columns of y's set bits, read from 8-bit chunk tables in shared memory):
+// writes are coalesced, reads follow the map. A CNot ring (the ansatz's entangler, a chain of
+// dependent gates the register-tile passes can only take two at a time) becomes one pass.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(ADJ_THREADS)
+k_linperm(const double2* __restrict__ src, double2* __restrict__ dst, uint64_t dim,
+          const uint64_t* __restrict__ tabs, int nchunks, uint64_t d) {
+    extern __shared__ uint64_t tsm[];
+    for (int i = threadIdx.x; i < nchunks * 256; i += ADJ_THREADS) tsm[i] = tabs[i];
+    __syncthreads();
+    for (uint64_t y = blockIdx.x * (uint64_t)ADJ_THREADS + threadIdx.x; y < dim;
+         y += (uint64_t)gridDim.x * ADJ_THREADS) {
+        uint64_t x = d;
+        for (int c = 0; c < nchunks; ++c) x ^= tsm[c * 256 + (int)((y >> (8 * c)) & 255u)];
+        dst[y] = src[x];
+    }
+}
+
+// Whether ops (applied in order) form an affine index map; if so, the gather tables of its
+// inverse: tabs[c * 256 + v] = xor of the inverse map's columns for the set bits of v (bits
+// 8c .. 8c+7), *d = inverse map of 0.
+static bool affine_tables(const qgpu_op* ops, size_t n_ops, int n, std::vector<uint64_t>* tabs,
+                          uint64_t* d) {
+    for (size_t g = 0; g < n_ops; ++g) {
+        const int k = ops[g].kind;
+        if (k != QGPU_GATE_CNOT && k != QGPU_GATE_X && k != QGPU_GATE_SWAP) return false;
+    }
+    // inverse of g_m ... g_1 is g_1 ... g_m (each gate is an involution): apply ops last to first
+    auto inv = [&](uint64_t y) {
+        for (size_t g = n_ops; g-- > 0;) {
+            const qgpu_op& op = ops[g];
+            const int t = n - 1 - op.target;
+            if (op.kind == QGPU_GATE_X) {
+                y ^= 1ull << t;
+            } else if (op.kind == QGPU_GATE_CNOT) {
+                const int c = n - 1 - op.controls[0];
+                y ^= ((y >> c) & 1ull) << t;
+            } else {  // Swap
+                const int c = n - 1 - op.controls[0];
+                const uint64_t bt = (y >> t) & 1ull, bc = (y >> c) & 1ull;
+                if (bt != bc) y ^= (1ull << t) | (1ull << c);
+            }
+        }
+        return y;
+    };
+    *d = inv(0);
+    std::vector<uint64_t> col(n);
+    for (int b = 0; b < n; ++b) col[b] = inv(1ull << b) ^ *d;
+    const int nchunks = (n + 7) / 8;
+    tabs->assign((size_t)nchunks * 256, 0);
+    for (int c = 0; c < nchunks; ++c)
+        for (int v = 0; v < 256; ++v) {
+            uint64_t x = 0;
+            for (int k = 0; k < 8; ++k)
+                if (((v >> k) & 1) && 8 * c + k < n) x ^= col[8 * c + k];
+            (*tabs)[(size_t)c * 256 + v] = x;
+        }
+    return true;
+}
+
 // grads[g] = sum over blocks of partial[g * nb + b], for g in [0, ng)
 __global__ void k_sum_partials(const double* __restrict__ partial, int nb, int ng,
                                double* __restrict__ out) {
@@ -477,8 +540,30 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
         if (is_rotation(ops[g].kind)) rot_slot[g] = (int)slot++;
     // reverse sweep
     std::vector<qgpu_op> seg;  // consecutive multi-wire gates, undone together
+    double2* spare = nullptr;  // third vector for out-of-place index permutations
     auto flush_seg = [&]() -> int {  // one plan for both vectors, launches queued without a sync
         if (seg.empty()) return QGPU_OK;
+        std::vector<uint64_t> tabs;
+        uint64_t d = 0;
+        if (h->n_qubits >= 10 && seg.size() >= 3 &&
+            affine_tables(seg.data(), seg.size(), h->n_qubits, &tabs, &d)) {
+            if (!spare && h->work3.ensure(vec) == QGPU_OK) spare = (double2*)h->work3.ptr;
+            if (spare && h->tables.ensure(tabs.size() * 8) == QGPU_OK) {
+                QGPU_CUDA(copy_async(h, h->tables.ptr, tabs.data(), tabs.size() * 8,
+                                     cudaMemcpyHostToDevice));
+                const int nch = (h->n_qubits + 7) / 8;
+                const int blocks = adj_blocks(h, h->dim);
+                for (double2** v : {&phi, &lam}) {
+                    k_linperm<<<blocks, ADJ_THREADS, nch * 256 * 8, h->stream>>>(
+                        *v, spare, h->dim, (const uint64_t*)h->tables.ptr, nch, d);
+                    QGPU_CHECK_LAUNCH("k_linperm");
+                    h->launches++;
+                    std::swap(*v, spare);
+                }
+                seg.clear();
+                return QGPU_OK;
+            }
+        }
         Plan plan;
         int s2 = build_plan(seg.data(), seg.size(), h->n_qubits, nullptr, 0, nullptr, 0,
                             plan_options_for(h), &plan);

@@ -60,6 +60,7 @@ struct qgpu_handle {
     qgpu::Scratch tables;      // per-program phase tables of fused diagonal runs
     qgpu::Scratch work;        // reductions, measurement buffers
     qgpu::Scratch work2;       // second buffer (measurement indices / adjoint vectors)
+    qgpu::Scratch work3;       // adjoint: target of out-of-place index permutations
     uint64_t launches = 0;     // kernels launched on this handle (for benchmarking claims)
     uint64_t h2d_bytes = 0;    // host->device traffic: copies + kernel parameter blocks
     uint64_t d2h_bytes = 0;    // device->host copies

@@ -311,6 +311,7 @@ int qgpu_destroy(qgpu_handle* h) {
     h->tables.release();
     h->work.release();
     h->work2.release();
+    h->work3.release();
     for (cudaEvent_t e : h->events) cudaEventDestroy(e);
     if (h->d_err) cudaFree(h->d_err);
     if (h->state) cudaFree(h->state);

@@ -72,6 +72,38 @@ def test_adjoint_all_gate_kinds_vs_oracle_fd(oracle):
     assert np.max(np.abs(g - fd)) <= 1e-7
 
 
+def test_adjoint_permutation_runs_vs_oracle_fd(oracle):
+    """Runs of CNot / X / Swap between rotation layers (undone as one index permutation each,
+    out of place): gradients against the oracle's finite differences, and the register still
+    holds the final state afterwards."""
+    n = 11
+    rng = np.random.default_rng(12)
+    b = ProgramBuilder(n)
+    for layer in range(3):
+        for w in range(n):
+            b.add("Ry", w, (), param=rng.uniform(-3, 3))
+            b.add("Rz", w, (), param=rng.uniform(-3, 3))
+        for w in range(n):
+            b.add("CNot", (w + 1) % n, (w,))      # ring: a chain of dependent gates
+        b.add("X", 3)
+        b.add("Swap", 2, (9,))
+        b.add("CNot", 0, (7,))
+        b.add("Swap", 5, (1,))
+        b.add("X", 10)
+    for w in range(n):
+        b.add("Rx", w, (), param=rng.uniform(-3, 3))
+    prog = b.build()
+    a_c = rng.normal(size=n)
+    b_c = rng.normal(size=n)
+    h = nat.Handle(n)
+    e, g = GR.energy_and_gradient(h, prog, a_c, b_c)
+    assert e == pytest.approx(_oracle_energy(oracle, prog, a_c, b_c), abs=1e-12)
+    fd = _oracle_fd(oracle, prog, a_c, b_c)
+    assert np.max(np.abs(g - fd)) <= 1e-7
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    assert np.max(np.abs(h.download() - ref)) <= 1e-12
+
+
 def test_adjoint_ansatz_20q_vs_fd_and_parameter_shift():
     """The differentiation config: 20 qubits, 10 layers of Ry Rz + CNot ring, 400 parameters."""
     an = W.ansatz(n=20, layers=10, seed=4)
