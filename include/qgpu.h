@@ -180,7 +180,8 @@ int qgpu_expectation_zzx(qgpu_handle* h, const double* a, const double* b, doubl
  * E = <psi_L|H|psi_L> and dE/dtheta for every op by the adjoint method: grads[g] is the
  * derivative with respect to the angle of op g when it is Rx, Ry, Rz or Phase, else 0.
  * Circuits with Custom gates are rejected with QGPU_ERR_NONUNITARY (their maps need not be
- * invertible). Uses two state-sized work vectors. */
+ * invertible). Uses two state-sized work vectors, and a third one when the circuit has runs of
+ * at least three CNot / X / Swap gates (each run is undone as one out-of-place index gather). */
 int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
                       const double* mats, size_t n_mat_doubles,
                       const uint8_t* none_flags, size_t n_none_flags,
