@@ -213,12 +213,11 @@ __global__ void __launch_bounds__(BLK_THREADS) k_block_ff(double2* __restrict__ 
 template <int D>
 static int launch_block_ff_t(qgpu_handle* h, const BlockArgs& a) {
     const size_t smem = (size_t)(D * D + D * BFF_GT) * 16;
-    static bool attr = false;
-    if (!attr) {
-        QGPU_CUDA(cudaFuncSetAttribute(k_block_ff<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-        attr = true;
-    }
+    // set once per kernel instance; a function-local static initialises once even when
+    // several host threads launch concurrently
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_block_ff<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    QGPU_CUDA(attr);
     const uint64_t ntiles = (a.ngroups + BFF_GT - 1) / BFF_GT;
     uint64_t blocks = std::min<uint64_t>(ntiles, (uint64_t)h->sm_count * 2);
     if (blocks < 1) blocks = 1;
@@ -244,12 +243,11 @@ static int launch_block_ff(qgpu_handle* h, const BlockArgs& a) {
 template <class T, int D>
 static int launch_block_t(qgpu_handle* h, const BlockArgs& a) {
     const size_t smem = (size_t)(D * D + D * BLK_GT) * sizeof(T);
-    static bool attr = false;
-    if (!attr) {
-        QGPU_CUDA(cudaFuncSetAttribute(k_block<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-        attr = true;
-    }
+    // set once per kernel instance; a function-local static initialises once even when
+    // several host threads launch concurrently
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_block<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    QGPU_CUDA(attr);
     const uint64_t ntiles = (a.ngroups + BLK_GT - 1) / BLK_GT;
     uint64_t blocks = std::min<uint64_t>(ntiles, (uint64_t)h->sm_count * 2);
     if (blocks < 1) blocks = 1;

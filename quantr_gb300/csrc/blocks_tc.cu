@@ -267,12 +267,11 @@ void build_bimg(const DenseBlock& b, std::vector<uint8_t>& img, size_t at) {
 template <int D>
 int launch_tc(qgpu_handle* h, const DenseBlock& b, const uint8_t* dev_img) {
     using SH = TcbShape<D>;
-    static bool attr = false;
-    if (!attr) {
-        QGPU_CUDA(cudaFuncSetAttribute(k_block_tc<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)SH::SMEM));
-        attr = true;
-    }
+    // set once per kernel instance; a function-local static initialises once even when
+    // several host threads launch concurrently
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_block_tc<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SH::SMEM);
+    QGPU_CUDA(attr);
     TcBlockArgs a;
     std::memset(&a, 0, sizeof(a));
     a.k = b.k;

@@ -837,12 +837,11 @@ template <class P>
 static int launch_tile1_pipe(qgpu_handle* h, const TileParams& p) {
     using S = typename P::S;
     const size_t smem = (size_t)PIPE_STAGES * 2 * PIPE_CH * sizeof(S);
-    static bool attr = false;
-    if (!attr) {
-        QGPU_CUDA(cudaFuncSetAttribute(k_tile1_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-        attr = true;
-    }
+    // set once per kernel instance; a function-local static initialises once even when
+    // several host threads launch concurrently
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_tile1_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    QGPU_CUDA(attr);
     const uint64_t nchunks = h->dim / (2ull * PIPE_CH);
     uint64_t blocks = std::min<uint64_t>(nchunks, (uint64_t)h->sm_count * 3);
     if (blocks < 1) blocks = 1;
