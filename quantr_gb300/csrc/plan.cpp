@@ -590,8 +590,8 @@ void emit_one(const AGate& g, std::vector<HStep>& out) {
 }
 
 // Tries to fold a run of diagonal steps into one TABLE step. Returns false when the run's bits
-// do not fit MAX_TABLE_FIELDS fields of MAX_TABLE_BITS contiguous bits.
-bool fold_table(const std::vector<HStep>& run, Plan* plan, HStep* out) {
+// do not fit MAX_TABLE_FIELDS fields of table_bits contiguous bits.
+bool fold_table(const std::vector<HStep>& run, Plan* plan, HStep* out, int table_bits) {
     uint64_t common = ~0ull;
     for (const HStep& h : run) common &= h.dcm;
     // bits each step depends on beyond the common condition
@@ -610,7 +610,7 @@ bool fold_table(const std::vector<HStep>& run, Plan* plan, HStep* out) {
         const int b = __builtin_ctzll(left);
         lo[nf] = b;
         int w = 0;
-        for (int q = b; q < 64 && q < b + MAX_TABLE_BITS; ++q)
+        for (int q = b; q < 64 && q < b + table_bits; ++q)
             if ((left >> q) & 1ull) w = q - b + 1;
         width[nf] = w;
         const uint64_t fm = (w >= 64) ? ~0ull : (((1ull << w) - 1ull) << b);
@@ -638,22 +638,47 @@ bool fold_table(const std::vector<HStep>& run, Plan* plan, HStep* out) {
     h.s.cm = common == ~0ull ? 0 : common;
     h.s.nfields = (uint8_t)nf;
     h.diagonal = true;
+    using cl = std::complex<long double>;
     for (int q = 0; q < nf; ++q) {
         const size_t entries = (size_t)1 << width[q];
         h.s.tab_off[q] = (uint32_t)(plan->table_f64.size() / 2);
         h.s.tab_shift[q] = (uint8_t)lo[q];
         h.s.tab_width[q] = (uint8_t)width[q];
+        std::vector<size_t> mine;  // the run's steps that live in this field
+        bool single = true;        // each one a factor on a single bit (a controlled phase)
+        for (size_t i = 0; i < run.size(); ++i) {
+            if (field[i] != q) continue;
+            mine.push_back(i);
+            const uint64_t need = run[i].dcm & ~common;
+            single = single && run[i].dfb < 0 && popcount64(need) == 1;
+        }
+        // single-bit factors: entry y is the product of the factors of y's set bits, built up
+        // from the entry without y's lowest bit (one multiply per entry)
+        std::vector<cl> tab(single ? entries : 0);
+        if (single) {
+            std::vector<cl> w(width[q], cl(1.0L, 0.0L));
+            for (size_t i : mine) {
+                const int b = __builtin_ctzll(run[i].dcm & ~common) - lo[q];
+                w[b] *= cl(run[i].d1.real(), run[i].d1.imag());
+            }
+            tab[0] = cl(1.0L, 0.0L);
+            for (size_t y = 1; y < entries; ++y)
+                tab[y] = tab[y & (y - 1)] * w[__builtin_ctzll(y)];
+        }
         for (size_t y = 0; y < entries; ++y) {
             const uint64_t idx = (uint64_t)y << lo[q];
-            std::complex<long double> acc(1.0L, 0.0L);
-            for (size_t i = 0; i < run.size(); ++i) {
-                if (field[i] != q) continue;
-                const HStep& s = run[i];
-                const uint64_t need = s.dcm & ~common;
-                if ((idx & need) != need) continue;
-                cd f = s.d1;
-                if (s.dfb >= 0) f = ((idx >> s.dfb) & 1ull) ? s.d1 : s.d0;
-                acc *= std::complex<long double>(f.real(), f.imag());
+            cl acc(1.0L, 0.0L);
+            if (single) {
+                acc = tab[y];
+            } else {
+                for (size_t i : mine) {
+                    const HStep& s = run[i];
+                    const uint64_t need = s.dcm & ~common;
+                    if ((idx & need) != need) continue;
+                    cd f = s.d1;
+                    if (s.dfb >= 0) f = ((idx >> s.dfb) & 1ull) ? s.d1 : s.d0;
+                    acc *= cl(f.real(), f.imag());
+                }
             }
             const cd v((double)acc.real(), (double)acc.imag());
             plan->table_f64.push_back(v.real());
@@ -824,7 +849,8 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
             }
             HStep t;
             std::vector<HStep> run(steps.begin() + i, steps.begin() + j);
-            if (general >= 2 && fold_table(run, plan, &t)) {
+            const int tb = std::max(1, std::min(opt.table_bits, MAX_TABLE_BITS));
+            if (general >= 2 && fold_table(run, plan, &t, tb)) {
                 folded.push_back(t);
                 folded_block.push_back(-1);
             } else {

@@ -49,7 +49,7 @@ enum StepType : uint8_t {
 constexpr int MAX_TILE_BITS = 3;
 constexpr int MAX_STEPS = 24;
 constexpr int MAX_TABLE_FIELDS = 3;
-constexpr int MAX_TABLE_BITS = 11;
+constexpr int MAX_TABLE_BITS = 14;  // widest table field the planner may form
 
 // Step as seen by the device: FF constants (re_h, re_l, im_h, im_l per complex), f64 and f32
 // copies, so one table serves every arithmetic policy.
@@ -125,6 +125,7 @@ struct PlanOptions {
     bool fuse_diagonal = true;         // fold diagonal runs into phase tables
     bool xor_runs = true;              // runs of >= 3 commuting controlled-X gates -> one pass
     bool pair_fusion = false;          // fuse gates on two wires into 4x4 blocks where cheaper
+    int table_bits = 11;               // width of a phase-table field (<= MAX_TABLE_BITS)
 };
 
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,

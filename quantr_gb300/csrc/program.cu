@@ -1297,6 +1297,7 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     o.max_arith_bits = o.policy == POL_FF ? env_int("QGPU_ARITH_TILE_BITS", 2) : MAX_TILE_BITS;
     // 4x4 pair blocks (k_pair) for the float-pair policy; QGPU_PAIR_FUSION=0 turns them off
     o.pair_fusion = o.policy == POL_FF && env_int("QGPU_PAIR_FUSION", 1) != 0;
+    o.table_bits = env_int("QGPU_TABLE_BITS", 11);  // tuning knob: phase-table field width
     return o;
 }
 
