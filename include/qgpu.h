@@ -126,7 +126,11 @@ int qgpu_download(qgpu_handle* h, double* interleaved_out, size_t n_amplitudes);
 /* ---- simulation ------------------------------------------------------------------------- */
 
 /* Applies ops[0..n_ops) in order: the loop of `simulate_with_register` (simulation.rs:37-56)
- * with one `apply_gate` (simulation.rs:64-135) per op. Identity ops are skipped. */
+ * with one `apply_gate` (simulation.rs:64-135) per op. Identity ops are skipped. In the fused
+ * modes the passes are queued on the handle's stream and the call returns once they are queued
+ * (the host can plan the next circuit meanwhile); every later call on the handle is ordered
+ * after them, and the ones that read results back (download, measure, norm, ...) wait for
+ * them. A device fault in a queued pass is reported by the next call that synchronises. */
 int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
                        const double* mats, size_t n_mat_doubles,
                        const uint8_t* none_flags, size_t n_none_flags);

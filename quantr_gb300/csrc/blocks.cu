@@ -312,13 +312,14 @@ static int apply_blocks_cc(qgpu_handle* h, const std::vector<DenseBlock>& blocks
     QGPU_CUDA(copy_async(h, h->tables.ptr, host.data(), total, cudaMemcpyHostToDevice));
     std::vector<std::string> names;
     std::vector<double> bytes;
+    size_t ev_base = 0;
     if (h->profile) {
-        st = prof_events(h, blocks.size());
+        st = prof_events(h, blocks.size(), &ev_base);
         if (st != QGPU_OK) return st;
     }
     for (size_t i = 0; i < blocks.size(); ++i) {
         if (h->profile) {
-            QGPU_CUDA(cudaEventRecord(h->events[2 * i], h->stream));
+            QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + i)], h->stream));
             names.push_back((ff ? "k_block_ff<" : "k_block<") + std::to_string(1 << blocks[i].k) + ">");
             bytes.push_back(2.0 * (double)h->amp_bytes * (double)h->dim);
         }
@@ -331,7 +332,7 @@ static int apply_blocks_cc(qgpu_handle* h, const std::vector<DenseBlock>& blocks
         st = ff ? launch_block_ff(h, a)
                 : (h->precision == QGPU_C128) ? launch_block<double2>(h, a) : launch_block<float2>(h, a);
         if (st != QGPU_OK) return st;
-        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * i + 1], h->stream));
+        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + i) + 1], h->stream));
     }
     if (h->profile) {
         st = prof_collect(h, names, bytes);

@@ -311,14 +311,15 @@ int apply_blocks_tc(qgpu_handle* h, const std::vector<DenseBlock>& blocks) {
     QGPU_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     std::vector<std::string> names;
     std::vector<double> bytes;
+    size_t ev_base = 0;
     if (h->profile) {
-        st = prof_events(h, blocks.size());
+        st = prof_events(h, blocks.size(), &ev_base);
         if (st != QGPU_OK) return st;
     }
     for (size_t i = 0; i < blocks.size(); ++i) {
         const uint8_t* dimg = (const uint8_t*)h->tables.ptr + offs[i];
         if (h->profile) {
-            QGPU_CUDA(cudaEventRecord(h->events[2 * i], h->stream));
+            QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + i)], h->stream));
             names.push_back("k_block_tc<" + std::to_string(1 << blocks[i].k) + ">");
             bytes.push_back(2.0 * (double)h->amp_bytes * (double)h->dim);
         }
@@ -329,7 +330,7 @@ int apply_blocks_tc(qgpu_handle* h, const std::vector<DenseBlock>& blocks) {
             default: st = launch_tc<64>(h, blocks[i], dimg); break;
         }
         if (st != QGPU_OK) return st;
-        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * i + 1], h->stream));
+        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + i) + 1], h->stream));
     }
     int err = 0;
     QGPU_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <map>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -67,6 +68,8 @@ struct qgpu_handle {
     // per-pass event profiling (qgpu_set_profiling)
     bool profile = false;
     std::vector<cudaEvent_t> events;
+    size_t ev_used = 0;        // event pairs recorded and not yet read back
+    std::vector<std::pair<std::string, double>> ev_pending;  // (kernel name, bytes) per pair
     struct ProfEntry {
         uint64_t launches = 0;
         double ms = 0.0;
@@ -85,11 +88,15 @@ inline cudaError_t copy_async(qgpu_handle* h, void* dst, const void* src, size_t
     if (kind == cudaMemcpyDeviceToHost) h->d2h_bytes += n;
     return cudaMemcpyAsync(dst, src, n, kind, h->stream);
 }
-// Event pair i of the handle's pool (grown on demand); nullptr when profiling is off.
-int prof_events(qgpu_handle* h, size_t pairs);
-// Reads back the recorded pairs and accumulates them under the given names.
+// Reserves `pairs` event pairs of the handle's pool (grown on demand); *base receives the index
+// of the first one (pair i = events[2 (base + i)], events[2 (base + i) + 1]).
+int prof_events(qgpu_handle* h, size_t pairs, size_t* base);
+// Files the reserved pairs under the given names; they are read back lazily (prof_flush), so
+// profiling adds no synchronisation to the calls it measures.
 int prof_collect(qgpu_handle* h, const std::vector<std::string>& names,
                  const std::vector<double>& bytes);
+// Waits for the stream and accumulates every pending pair into the per-kernel totals.
+int prof_flush(qgpu_handle* h);
 }  // namespace qgpu
 
 // ---------------------------------------------------------------------------------------------

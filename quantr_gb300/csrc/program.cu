@@ -1027,6 +1027,13 @@ static int launch_xor(qgpu_handle* h, const XorPerm& xp) {
 
 static int env_int(const char* name, int dflt);
 
+// Bulk-copy staging for 1-bit tiles (QGPU_PIPE=1). Its kernel reports bounded-wait timeouts
+// through the handle's error word, so plans run with it are synchronised at the end.
+static int pipe_enabled() {
+    static const int on = env_int("QGPU_PIPE", 0);
+    return on;
+}
+
 template <int K, int U, class P>
 static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
     const uint64_t per_block = 256ull * U;
@@ -1073,7 +1080,7 @@ static int launch_tile_k(qgpu_handle* h, const TileParams& p) {
     // Bulk-copy staging for 1-bit tiles (k_tile1_pipe): correct and measured, but on GB300 its
     // shared-memory footprint lowers occupancy below what the float-pair arithmetic needs, so the
     // register-tile kernel stays the default (QGPU_PIPE=1 selects the pipeline).
-    static const int use_pipe = env_int("QGPU_PIPE", 0);
+    static const int use_pipe = pipe_enabled();
     switch (p.nbits) {
         case 1:
             if (use_pipe && h->n_qubits >= 13) return launch_tile1_pipe<P>(h, p);
@@ -1197,8 +1204,9 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
     std::vector<std::string> prof_names;
     std::vector<double> prof_bytes;
     const size_t nlaunch = plan.passes.size() + (resident ? 2 : 0);
+    size_t ev_base = 0;
     if (h->profile) {
-        int st = prof_events(h, nlaunch);
+        int st = prof_events(h, nlaunch, &ev_base);
         if (st != QGPU_OK) return st;
     }
     static const char* pol_name[] = {"ff", "f64", "f32"};
@@ -1210,7 +1218,7 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
         const bool last_conv = resident && li == nlaunch - 1;
         const Pass* ps = (first_conv || last_conv) ? nullptr : &plan.passes[li - (resident ? 1 : 0)];
         if (h->profile) {
-            QGPU_CUDA(cudaEventRecord(h->events[2 * li], h->stream));
+            QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + li)], h->stream));
             if (!ps) {
                 prof_names.push_back("k_ff_layout");
             } else if (ps->pair >= 0) {
@@ -1239,12 +1247,13 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
             st = launch_pass(h, *ps, pol, resident, tab_ff, tab_f64, tp);
         }
         if (st != QGPU_OK) return st;
-        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * li + 1], h->stream));
+        if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + li) + 1], h->stream));
     }
-    if (!sync && !h->profile) return QGPU_OK;  // the caller synchronises the stream later
+    int st = h->profile ? prof_collect(h, prof_names, prof_bytes) : QGPU_OK;
+    if (st != QGPU_OK) return st;
+    if (!sync) return QGPU_OK;  // queued; later calls on the stream are ordered after it
     int err = 0;
     QGPU_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    int st = h->profile ? prof_collect(h, prof_names, prof_bytes) : QGPU_OK;
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
     if (err) return fail(QGPU_ERR_TIMEOUT, "a pipelined pass gave up waiting for its bulk copies");
     return st;
@@ -1362,7 +1371,8 @@ extern "C" int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_o
     int st = build_plan(ops, n_ops, h->n_qubits, mats, n_mat_doubles, none_flags, n_none_flags,
                         plan_options_for(h), &plan);
     if (st != QGPU_OK) return st;
-    return run_plan(h, plan);
+    // queued without a final synchronisation unless the plan can report a bounded-wait timeout
+    return run_plan(h, plan, pipe_enabled() != 0);
 }
 
 // One CTA waits, with the pipelined kernels' bounded poll, on an mbarrier phase that nothing

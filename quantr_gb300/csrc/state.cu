@@ -169,26 +169,41 @@ int reduce_state(qgpu_handle* h, int what, double2* host_out) {
     return QGPU_OK;
 }
 
-int prof_events(qgpu_handle* h, size_t pairs) {
-    while (h->events.size() < 2 * pairs) {
+int prof_flush(qgpu_handle* h) {
+    if (h->ev_pending.empty()) return QGPU_OK;
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < h->ev_pending.size(); ++i) {
+        float ms = 0.f;
+        QGPU_CUDA(cudaEventElapsedTime(&ms, h->events[2 * i], h->events[2 * i + 1]));
+        qgpu_handle::ProfEntry& e = h->prof[h->ev_pending[i].first];
+        e.launches += 1;
+        e.ms += ms;
+        e.bytes += h->ev_pending[i].second;
+    }
+    h->ev_pending.clear();
+    h->ev_used = 0;
+    return QGPU_OK;
+}
+
+int prof_events(qgpu_handle* h, size_t pairs, size_t* base) {
+    constexpr size_t MAX_PENDING_PAIRS = 16384;  // read back before the pool grows past this
+    if (h->ev_used + pairs > MAX_PENDING_PAIRS) {
+        int st = prof_flush(h);
+        if (st != QGPU_OK) return st;
+    }
+    while (h->events.size() < 2 * (h->ev_used + pairs)) {
         cudaEvent_t e;
         QGPU_CUDA(cudaEventCreate(&e));
         h->events.push_back(e);
     }
+    *base = h->ev_used;
     return QGPU_OK;
 }
 
 int prof_collect(qgpu_handle* h, const std::vector<std::string>& names,
                  const std::vector<double>& bytes) {
-    QGPU_CUDA(cudaStreamSynchronize(h->stream));
-    for (size_t i = 0; i < names.size(); ++i) {
-        float ms = 0.f;
-        QGPU_CUDA(cudaEventElapsedTime(&ms, h->events[2 * i], h->events[2 * i + 1]));
-        qgpu_handle::ProfEntry& e = h->prof[names[i]];
-        e.launches += 1;
-        e.ms += ms;
-        e.bytes += bytes[i];
-    }
+    for (size_t i = 0; i < names.size(); ++i) h->ev_pending.emplace_back(names[i], bytes[i]);
+    h->ev_used += names.size();
     return QGPU_OK;
 }
 
@@ -220,6 +235,8 @@ int qgpu_set_profiling(qgpu_handle* h, int on) {
 
 int qgpu_profile_json(qgpu_handle* h, char* buf, size_t cap, int reset) {
     if (!h || (!buf && cap)) return fail(QGPU_ERR_INVALID, "qgpu_profile_json: NULL argument");
+    int st = prof_flush(h);
+    if (st != QGPU_OK) return st;
     std::string s = "{";
     bool first = true;
     for (const auto& kv : h->prof) {
