@@ -228,6 +228,7 @@ def run_precision(args) -> None:
             h.profile(reset=True)
             t0 = time.perf_counter()
             h.apply(prog.ops, prog.mats, prog.none)
+            h.synchronize()
             wall = time.perf_counter() - t0
             prof = h.profile(reset=True)
             nrm = h.norm()

@@ -135,6 +135,10 @@ int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
                        const double* mats, size_t n_mat_doubles,
                        const uint8_t* none_flags, size_t n_none_flags);
 
+/* Waits until every operation queued on the handle's stream has finished; returns the status of
+ * that work (a device fault in a queued pass surfaces here). No counterpart in quantr. */
+int qgpu_synchronize(qgpu_handle* h);
+
 /* ---- measurement ------------------------------------------------------------------------ */
 
 /* `SimulatedCircuit::measure_all(shots)` (simulated_circuit.rs:63-73): `shots` draws of

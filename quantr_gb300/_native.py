@@ -66,6 +66,7 @@ _EXPORTS = {
     "qgpu_extract_nonzero": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_size_t,
                                        C.POINTER(C.c_size_t)]),
     "qgpu_norm": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "qgpu_synchronize": (C.c_int, [C.c_void_p]),
     "qgpu_checksum": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "qgpu_expectation_zzx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "qgpu_adjoint_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
@@ -201,6 +202,10 @@ class Handle:
         check(lib().qgpu_extract_nonzero(self._h, float(margin), ptr(idx), ptr(amp), cap,
                                          C.byref(cnt)), "qgpu_extract_nonzero")
         return idx[:cnt.value].copy(), amp[:cnt.value].copy()
+
+    def synchronize(self) -> None:
+        """Wait for every queued pass (apply returns once its passes are queued)."""
+        check(lib().qgpu_synchronize(self._h), "qgpu_synchronize")
 
     def norm(self) -> float:
         v = C.c_double()

@@ -1119,7 +1119,54 @@ static int launch_ff_layout(qgpu_handle* h, bool to_pairs) {
     return QGPU_OK;
 }
 
+// complex64 pair blocks: the 4x4 in f32 FMA, 16 complex multiply-adds per quad (memory-bound)
+struct PairParams32 {
+    uint64_t ngroups;
+    int lo, hi;
+    float2 m[4][4];  // m[out][in]
+};
+
+__global__ void __launch_bounds__(256) k_pair_f32(float2* __restrict__ st,
+                                                  const __grid_constant__ PairParams32 p) {
+    const uint64_t olo = 1ull << p.lo, ohi = 1ull << p.hi;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < p.ngroups; g += stride) {
+        const uint64_t b = insert_zero(insert_zero(g, p.lo), p.hi);
+        const uint64_t idx[4] = {b, b | olo, b | ohi, b | olo | ohi};
+        float2 x[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) x[j] = st[idx[j]];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            float re = 0.f, im = 0.f;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float2 u = p.m[r][c];
+                re = fmaf(u.x, x[c].x, fmaf(-u.y, x[c].y, re));
+                im = fmaf(u.x, x[c].y, fmaf(u.y, x[c].x, im));
+            }
+            st[idx[r]] = make_float2(re, im);
+        }
+    }
+}
+
 static int launch_pair(qgpu_handle* h, const PairBlock& pb, bool resident) {
+    if (h->precision == QGPU_C64) {
+        PairParams32 q;
+        q.ngroups = h->dim >> 2;
+        q.lo = pb.lo;
+        q.hi = pb.hi;
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c)
+                q.m[r][c] = make_float2((float)pb.m[r][c].real(), (float)pb.m[r][c].imag());
+        uint64_t blocks = std::min<uint64_t>((q.ngroups + 255) / 256, (uint64_t)h->sm_count * 8);
+        if (blocks < 1) blocks = 1;
+        k_pair_f32<<<(unsigned)blocks, 256, 0, h->stream>>>((float2*)cur_state(h), q);
+        QGPU_CHECK_LAUNCH("k_pair_f32");
+        h->launches++;
+        h->h2d_bytes += sizeof(PairParams32);
+        return QGPU_OK;
+    }
     PairParams p;
     p.ngroups = h->dim >> 2;
     p.lo = pb.lo;
@@ -1222,7 +1269,9 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
             if (!ps) {
                 prof_names.push_back("k_ff_layout");
             } else if (ps->pair >= 0) {
-                prof_names.push_back(resident ? "k_pair<ffr>" : "k_pair<ff>");
+                prof_names.push_back(h->precision == QGPU_C64 ? "k_pair<f32>"
+                                     : resident               ? "k_pair<ffr>"
+                                                              : "k_pair<ff>");
             } else if (ps->custom >= 0) {
                 prof_names.push_back("k_group");
             } else if (ps->xor_pass) {
@@ -1305,7 +1354,7 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     // keep arithmetic passes at 2 tile bits
     o.max_arith_bits = o.policy == POL_FF ? env_int("QGPU_ARITH_TILE_BITS", 2) : MAX_TILE_BITS;
     // 4x4 pair blocks (k_pair) for the float-pair policy; QGPU_PAIR_FUSION=0 turns them off
-    o.pair_fusion = o.policy == POL_FF && env_int("QGPU_PAIR_FUSION", 1) != 0;
+    o.pair_fusion = (o.policy == POL_FF || o.policy == POL_F32) && env_int("QGPU_PAIR_FUSION", 1) != 0;
     o.table_bits = env_int("QGPU_TABLE_BITS", 11);  // tuning knob: phase-table field width
     return o;
 }

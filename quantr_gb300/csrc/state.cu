@@ -227,6 +227,12 @@ int qgpu_io_bytes(const qgpu_handle* h, uint64_t* h2d, uint64_t* d2h) {
     return QGPU_OK;
 }
 
+int qgpu_synchronize(qgpu_handle* h) {
+    if (!h) return fail(QGPU_ERR_INVALID, "qgpu_synchronize: NULL handle");
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    return QGPU_OK;
+}
+
 int qgpu_set_profiling(qgpu_handle* h, int on) {
     if (!h) return fail(QGPU_ERR_INVALID, "qgpu_set_profiling: NULL handle");
     h->profile = on != 0;
