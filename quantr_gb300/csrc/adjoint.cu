@@ -22,7 +22,9 @@
 namespace qgpu {
 
 int apply_ops_on(qgpu_handle* h, void* buffer, const qgpu_op* ops, size_t n_ops);  // program.cu
-int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync);         // program.cu
+int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync,
+                bool pre_resident);                                                 // program.cu
+int ff_layout_on(qgpu_handle* h, void* buffer, bool to_pairs);                      // program.cu
 PlanOptions plan_options_for(const qgpu_handle* h);
 
 constexpr int ADJ_THREADS = 256;
@@ -257,7 +259,7 @@ __device__ __forceinline__ void adj_tile_step(ffp* f, ffp* l, const AdjTileStep&
     }
 }
 
-template <int K>
+template <int K, bool FFR>
 __global__ void __launch_bounds__(ADJ_THREADS)
 k_adj_tile(double2* __restrict__ phi, double2* __restrict__ lam,
            const __grid_constant__ AdjTileParams p, double* __restrict__ partial) {
@@ -288,8 +290,8 @@ k_adj_tile(double2* __restrict__ phi, double2* __restrict__ lam,
         ffp f[T], l[T];
 #pragma unroll
         for (int j = 0; j < T; ++j) {
-            f[j] = to_ffp(phi[b | off[j]]);
-            l[j] = to_ffp(lam[b | off[j]]);
+            f[j] = FFR ? ffr_load(phi[b | off[j]]) : to_ffp(phi[b | off[j]]);
+            l[j] = FFR ? ffr_load(lam[b | off[j]]) : to_ffp(lam[b | off[j]]);
         }
 #pragma unroll
         for (int s = 0; s < ADJ_TILE_STEPS; ++s) {
@@ -301,8 +303,8 @@ k_adj_tile(double2* __restrict__ phi, double2* __restrict__ lam,
         }
 #pragma unroll
         for (int j = 0; j < T; ++j) {
-            phi[b | off[j]] = from_ffp(f[j]);
-            lam[b | off[j]] = from_ffp(l[j]);
+            phi[b | off[j]] = FFR ? ffr_store(f[j]) : from_ffp(f[j]);
+            lam[b | off[j]] = FFR ? ffr_store(l[j]) : from_ffp(l[j]);
         }
     }
 #pragma unroll
@@ -332,7 +334,8 @@ k_adj_tile(double2* __restrict__ phi, double2* __restrict__ lam,
 template <int K>
 static int launch_adj_tile(qgpu_handle* h, double2* phi, double2* lam, const AdjTileParams& p,
                            double* partial) {
-    k_adj_tile<K><<<p.nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, p, partial);
+    // phi and lambda stay in the resident float-pair layout for the whole sweep
+    k_adj_tile<K, true><<<p.nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, p, partial);
     QGPU_CHECK_LAUNCH("k_adj_tile");
     h->launches++;
     h->h2d_bytes += sizeof(AdjTileParams);
@@ -533,6 +536,14 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
     QGPU_CUDA(cudaMemcpyAsync(phi, h->state, vec, cudaMemcpyDeviceToDevice, h->stream));
     st = energy_into(h, phi, lam, H, partial + nrot * (size_t)nb, energy);
     if (st != QGPU_OK) return st;
+    // QGPU_MODE_FAST: the sweep works on phi and lambda in the resident float-pair layout (one
+    // conversion each here; the vectors are scratch, nothing converts them back)
+    const bool tiles = h->mode == QGPU_MODE_FAST;
+    if (tiles) {
+        st = ff_layout_on(h, phi, true);
+        if (st == QGPU_OK) st = ff_layout_on(h, lam, true);
+        if (st != QGPU_OK) return st;
+    }
 
     std::vector<int> rot_slot(n_ops, -1);
     size_t slot = 0;
@@ -567,8 +578,8 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
         Plan plan;
         int s2 = build_plan(seg.data(), seg.size(), h->n_qubits, nullptr, 0, nullptr, 0,
                             plan_options_for(h), &plan);
-        if (s2 == QGPU_OK) s2 = run_plan_on(h, phi, plan, false);
-        if (s2 == QGPU_OK) s2 = run_plan_on(h, lam, plan, false);
+        if (s2 == QGPU_OK) s2 = run_plan_on(h, phi, plan, false, tiles);
+        if (s2 == QGPU_OK) s2 = run_plan_on(h, lam, plan, false, tiles);
         seg.clear();
         return s2;
     };
@@ -646,7 +657,6 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
         }
         return launch();
     };
-    const bool tiles = h->mode == QGPU_MODE_FAST;
     for (size_t gi = n_ops; gi-- > 0;) {
         const qgpu_op& op = ops[gi];
         if (op.kind == QGPU_GATE_ID) continue;

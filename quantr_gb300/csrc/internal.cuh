@@ -274,6 +274,18 @@ __device__ __forceinline__ double2 from_ffp(const ffp& v) {
     return make_double2(join_f64(rh, rl), join_f64(ih, il));
 }
 
+// Resident float-pair layout: a 16-byte amplitude slot holds (re_h, im_h | re_l, im_l), read and
+// written as the two packed registers of an ffp.
+__device__ __forceinline__ ffp ffr_load(double2 a) {
+    ffp r;
+    r.h = (u64)__double_as_longlong(a.x);
+    r.l = (u64)__double_as_longlong(a.y);
+    return r;
+}
+__device__ __forceinline__ double2 ffr_store(const ffp& r) {
+    return make_double2(__longlong_as_double((long long)r.h), __longlong_as_double((long long)r.l));
+}
+
 // Dot2 on both lanes at once. A term's constants are c[0..3] = (U_hi, U_lo, -U_hi, -U_lo);
 // `en` holds the negated error sum so that every update is a single fma/add/sub.
 struct PDot2 {

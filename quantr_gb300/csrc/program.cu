@@ -376,15 +376,6 @@ struct PolRaw {
 // amplitude slot holds (re_h, im_h | re_l, im_l) instead of (re, im) as doubles. Loads and stores
 // are then plain register moves (no split, no join on the FP64 pipe); k_ff_layout converts the
 // whole register once before the run and once after it.
-__device__ __forceinline__ ffp ffr_load(double2 a) {
-    ffp r;
-    r.h = (u64)__double_as_longlong(a.x);
-    r.l = (u64)__double_as_longlong(a.y);
-    return r;
-}
-__device__ __forceinline__ double2 ffr_store(const ffp& r) {
-    return make_double2(__longlong_as_double((long long)r.h), __longlong_as_double((long long)r.l));
-}
 
 struct PolFFR : PolFF {
     static __device__ __forceinline__ R load(S a) { return ffr_load(a); }
@@ -1208,9 +1199,12 @@ static bool plan_resident(const qgpu_handle* h, const Plan& plan) {
     return arith >= 8;
 }
 
-static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
+// pre_resident: the buffer already holds the resident float-pair layout (the adjoint sweep keeps
+// its vectors that way); the passes use it as is and no layout conversion is launched.
+static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre_resident = false) {
     const int pol = policy_of(h);
-    const bool resident = plan_resident(h, plan);
+    const bool resident = pre_resident || plan_resident(h, plan);
+    const bool convert = resident && !pre_resident;
     // phase tables for every TABLE step of the plan, uploaded once
     const size_t nent = plan.table_f64.size() / 2;
     const float4* tab_ff = nullptr;
@@ -1250,7 +1244,7 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
     TileParams tp;
     std::vector<std::string> prof_names;
     std::vector<double> prof_bytes;
-    const size_t nlaunch = plan.passes.size() + (resident ? 2 : 0);
+    const size_t nlaunch = plan.passes.size() + (convert ? 2 : 0);
     size_t ev_base = 0;
     if (h->profile) {
         int st = prof_events(h, nlaunch, &ev_base);
@@ -1261,9 +1255,9 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true) {
     const double full_bytes = 2.0 * (double)h->amp_bytes * (double)h->dim;
     for (size_t li = 0; li < nlaunch; ++li) {
         // launch li: [layout to pairs], passes..., [layout back]
-        const bool first_conv = resident && li == 0;
-        const bool last_conv = resident && li == nlaunch - 1;
-        const Pass* ps = (first_conv || last_conv) ? nullptr : &plan.passes[li - (resident ? 1 : 0)];
+        const bool first_conv = convert && li == 0;
+        const bool last_conv = convert && li == nlaunch - 1;
+        const Pass* ps = (first_conv || last_conv) ? nullptr : &plan.passes[li - (convert ? 1 : 0)];
         if (h->profile) {
             QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + li)], h->stream));
             if (!ps) {
@@ -1364,21 +1358,31 @@ int apply_blocks(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double*
 
 // Runs non-Custom ops as fused passes on `buffer` (a state-sized device vector of the handle's
 // precision) instead of the register.
-int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync);
+int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync, bool pre_resident);
 
 int apply_ops_on(qgpu_handle* h, void* buffer, const qgpu_op* ops, size_t n_ops) {
     Plan plan;
     int st = build_plan(ops, n_ops, h->n_qubits, nullptr, 0, nullptr, 0, plan_options_for(h), &plan);
     if (st != QGPU_OK) return st;
-    return run_plan_on(h, buffer, plan, true);
+    return run_plan_on(h, buffer, plan, true, false);
 }
 
 // Runs an already built plan (no Custom gates) on `buffer`; with sync = false the launches are
-// only queued on the handle's stream (the plan's tables are copied before this returns).
-int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync) {
+// only queued on the handle's stream (the plan's tables are copied before this returns). With
+// pre_resident the buffer is in the resident float-pair layout and stays in it.
+int run_plan_on(qgpu_handle* h, void* buffer, const Plan& plan, bool sync, bool pre_resident) {
     void* saved = h->active;
     h->active = buffer;
-    const int st = run_plan(h, plan, sync);
+    const int st = run_plan(h, plan, sync, pre_resident);
+    h->active = saved;
+    return st;
+}
+
+// Converts a complex128 work vector to the resident float-pair layout or back, in place.
+int ff_layout_on(qgpu_handle* h, void* buffer, bool to_pairs) {
+    void* saved = h->active;
+    h->active = buffer;
+    const int st = launch_ff_layout(h, to_pairs);
     h->active = saved;
     return st;
 }
