@@ -125,7 +125,7 @@ struct PlanOptions {
     bool fuse_diagonal = true;         // fold diagonal runs into phase tables
     bool xor_runs = true;              // runs of >= 3 commuting controlled-X gates -> one pass
     bool pair_fusion = false;          // fuse gates on two wires into 4x4 blocks where cheaper
-    int table_bits = 11;               // width of a phase-table field (<= MAX_TABLE_BITS)
+    int table_bits = 10;               // width of a phase-table field (<= MAX_TABLE_BITS)
 };
 
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,

@@ -208,6 +208,7 @@ struct TileParams {
     const float4* tab_ff;     // TABLE entries, float pairs
     const double2* tab_f64;   // TABLE entries, f64
     int prefetch;             // prefetch the next grid-stride iteration into L2
+    int streaming;            // register loads/stores with the evict-first (streaming) hint
     int nbits;
     int bits[MAX_TILE_BITS];
     int nsteps;
@@ -635,6 +636,18 @@ __device__ __forceinline__ void step_tile(typename P::R* v, const DevStep& s, ui
     }
 }
 
+// Register traffic of the tile kernels; with `streaming` the cache-streaming forms keep the
+// once-touched amplitudes from evicting phase-table lines out of L1.
+template <class S>
+__device__ __forceinline__ S tile_load(const S* p, int streaming) {
+    return streaming ? __ldcs(p) : *p;
+}
+template <class S>
+__device__ __forceinline__ void tile_store(S* p, S v, int streaming) {
+    if (streaming) __stcs(p, v);
+    else *p = v;
+}
+
 // ONE >= 0: the pass is exactly one unconditional step of that type on tile bit 0 (the common
 // single fused gate), applied as straight-line code without the step loop or its dispatch.
 template <int K, int U, class P, int ONE = -1>
@@ -662,7 +675,7 @@ __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, co
             base[u] = b;
             if (g < p.ngroups) {
 #pragma unroll
-                for (int j = 0; j < T; ++j) raw[u][j] = st[b | off[j]];
+                for (int j = 0; j < T; ++j) raw[u][j] = tile_load(st + (b | off[j]), p.streaming);
             }
         }
         if (p.prefetch) {  // the next iteration's amplitudes head for L2 while this one computes
@@ -720,7 +733,7 @@ __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, co
             const uint64_t g = g0 + (uint64_t)u * blockDim.x + threadIdx.x;
             if (g >= p.ngroups) continue;
 #pragma unroll
-            for (int j = 0; j < T; ++j) st[base[u] | off[j]] = P::store(v[u][j]);
+            for (int j = 0; j < T; ++j) tile_store(st + (base[u] | off[j]), P::store(v[u][j]), p.streaming);
         }
     }
 }
@@ -1317,6 +1330,12 @@ static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, bool resident,
         // for the dense pass on the same box): off unless QGPU_PREFETCH=1
         static const int prefetch = env_int("QGPU_PREFETCH", 0);
         tp.prefetch = prefetch;
+        // streaming hints for passes that read phase tables (tuning knob QGPU_TILE_STREAMING:
+        // 0 never, 1 passes with a TABLE step, 2 every pass)
+        static const int streaming = env_int("QGPU_TILE_STREAMING", 1);
+        bool has_table = false;
+        for (const DevStep& d : ps.steps) has_table = has_table || d.type == ST_TABLE;
+        tp.streaming = streaming == 2 || (streaming == 1 && has_table);
         int st;
         if (resident) {
             st = ps.arith ? launch_tile_k<PolFFR>(h, tp) : launch_tile_k<PolRawFFR>(h, tp);
@@ -1349,7 +1368,9 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     o.max_arith_bits = o.policy == POL_FF ? env_int("QGPU_ARITH_TILE_BITS", 2) : MAX_TILE_BITS;
     // 4x4 pair blocks (k_pair) for the float-pair policy; QGPU_PAIR_FUSION=0 turns them off
     o.pair_fusion = (o.policy == POL_FF || o.policy == POL_F32) && env_int("QGPU_PAIR_FUSION", 1) != 0;
-    o.table_bits = env_int("QGPU_TABLE_BITS", 11);  // tuning knob: phase-table field width
+    // phase-table field width (tuning knob QGPU_TABLE_BITS): 10 bits measured best on GB300 for
+    // the 30-qubit QFT rows (1114 ms per step; 11: 1118, 12: 1156, 9: 1182 ms)
+    o.table_bits = env_int("QGPU_TABLE_BITS", 10);
     return o;
 }
 
