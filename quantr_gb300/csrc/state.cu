@@ -86,13 +86,9 @@ __global__ void k_f2d(const float2* __restrict__ in, double2* __restrict__ out, 
 // Deterministic reductions: block b sums a fixed contiguous range with a fixed tree.
 constexpr int RED_THREADS = 256;
 
-template <class T>
-__device__ __forceinline__ double2 red_load(const T* s, uint64_t i, int what) {
-    double re = (double)s[i].x, im = (double)s[i].y;
-    if (what == 0) return make_double2(__dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)), 0.0);
-    return make_double2(re, im);
-}
-
+// what = 0 keeps |re|^2 and |im|^2 in two fused multiply-add chains (two FP64 operations per
+// amplitude; the FP64 pipe, not HBM, bounded the separate multiply/add form) and folds them
+// together once per thread; what = 1 sums re and im.
 template <class T>
 __global__ void k_reduce_partial(const T* __restrict__ s, uint64_t dim, uint64_t per_block,
                                  int what, double2* __restrict__ partial) {
@@ -101,10 +97,19 @@ __global__ void k_reduce_partial(const T* __restrict__ s, uint64_t dim, uint64_t
     uint64_t end = begin + per_block;
     if (end > dim) end = dim;
     double ax = 0.0, ay = 0.0;
-    for (uint64_t i = begin + threadIdx.x; i < end; i += RED_THREADS) {
-        double2 v = red_load(s, i, what);
-        ax += v.x;
-        ay += v.y;
+    if (what == 0) {
+        for (uint64_t i = begin + threadIdx.x; i < end; i += RED_THREADS) {
+            const double re = (double)s[i].x, im = (double)s[i].y;
+            ax = fma(re, re, ax);
+            ay = fma(im, im, ay);
+        }
+        ax += ay;
+        ay = 0.0;
+    } else {
+        for (uint64_t i = begin + threadIdx.x; i < end; i += RED_THREADS) {
+            ax += (double)s[i].x;
+            ay += (double)s[i].y;
+        }
     }
     sh[threadIdx.x] = make_double2(ax, ay);
     __syncthreads();
