@@ -18,7 +18,9 @@ Units (GB/s):
   pct_peak    bytes the engine's passes actually move (2 * 16 B * amplitudes each pass may
               change) per second, over the measured HBM peak.
   roofline    the dominant kernel: its per-launch algorithmic bytes / its average CUDA-event
-              duration, against the measured HBM peak (MEASURED_PEAKS.json).
+              duration, against the measured HBM peak (MEASURED_PEAKS.json). For the float-pair
+              pair-block kernels, which the FP32 pipe bounds, roofline.compute adds their lane
+              operations per second against the nominal FP32 lane rate.
   e2e         the same gate-apply GB/s through the public API (Circuit.simulate + measure_all of
               10^6 shots + norm), program upload and histogram download inside the timed region.
 
@@ -385,6 +387,22 @@ def run_ours(args) -> None:
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": peaks["source"], "launches_per_step": dom_launches / args.steps,
                 "share_of_step": dom_ms / args.steps / ms}
+    # The float-pair pair-block kernels are bound by the FP32 pipe rather than HBM: one 4x4
+    # complex block costs 91 packed f32x2 instructions (182 lane operations) per amplitude, and a
+    # k_pair2 launch applies two blocks. Their compute roofline is against the nominal FP32 lane
+    # rate at the sampled SM clock (152 SMs x 128 lanes).
+    blocks_per_launch = {"k_pair<ffr>": 1, "k_pair<ff>": 1, "k_pair2<ffr>": 2, "k_pair2<ff>": 2}
+    if dom_name in blocks_per_launch:
+        csum = clocks.summary()
+        mhz = csum.get("sm_mhz") or 2070.0
+        lane_ops = 182.0 * (1 << args.n) * blocks_per_launch[dom_name]
+        tops = lane_ops / (dom_ms / dom_launches / 1e3) / 1e12
+        peak_tops = 152 * 128 * mhz * 1e6 / 1e12
+        roofline["compute"] = {
+            "pipe": "FP32 (float-pair Dot2 in packed f32x2)", "achieved": tops, "peak": peak_tops,
+            "unit": "T lane-op/s", "frac": tops / peak_tops,
+            "ops_per_amplitude_per_block": 182, "blocks_per_launch": blocks_per_launch[dom_name],
+            "peak_source": f"nominal: 152 SMs x 128 FP32 lanes x {mhz:.0f} MHz (sampled SM clock)"}
     kernels = {k: {"launches_per_step": v[0] / args.steps, "ms_per_step": v[1] / args.steps,
                    "GBps": (v[2] / (v[1] / 1e3) / 1e9) if v[1] > 0 else None}
                for k, v in prof.items()}

@@ -694,6 +694,231 @@ bool fold_table(const std::vector<HStep>& run, Plan* plan, HStep* out, int table
 
 }  // namespace
 
+std::vector<XTerm> xor_terms(const XorPerm& xp) {
+    std::vector<XTerm> out;
+    for (int e = 0; e < xp.nterms; ++e) {
+        if (xp.grouped[e] == 2) {
+            XTerm t;
+            t.cm = t.flip = xp.cm[e];
+            t.swap = true;
+            out.push_back(t);
+        } else if (xp.grouped[e] == 1) {  // controls at target + shift
+            for (int c = 0; c < 64; ++c)
+                if ((xp.cm[e] >> c) & 1ull) {
+                    XTerm t;
+                    t.cm = 1ull << c;
+                    t.flip = 1ull << (c - xp.shift[e]);
+                    out.push_back(t);
+                }
+        } else {
+            XTerm t;
+            t.cm = xp.cm[e];
+            t.flip = xp.tbit[e];
+            out.push_back(t);
+        }
+    }
+    return out;
+}
+
+bool xor_from_terms(const std::vector<XTerm>& ts, XorPerm* xp) {
+    *xp = XorPerm();
+    for (const XTerm& t : ts) {
+        int g = -1;
+        if (t.swap) {
+            if (xp->nterms == MAX_XOR_TERMS) return false;
+            g = xp->nterms++;
+            xp->grouped[g] = 2;
+            xp->shift[g] = 0;
+            xp->cm[g] = t.cm;
+            xp->tbit[g] = 0;
+            continue;
+        }
+        if (popcount64(t.cm) == 1) {
+            const int shift = __builtin_ctzll(t.cm) - __builtin_ctzll(t.flip);
+            for (int e = 0; e < xp->nterms; ++e)
+                if (xp->grouped[e] == 1 && xp->shift[e] == shift) g = e;
+            if (g < 0) {
+                if (xp->nterms == MAX_XOR_TERMS) return false;
+                g = xp->nterms++;
+                xp->grouped[g] = 1;
+                xp->shift[g] = shift;
+                xp->cm[g] = 0;
+                xp->tbit[g] = 0;
+            }
+            xp->cm[g] |= t.cm;
+            xp->tbit[g] |= t.flip;
+            continue;
+        }
+        if (xp->nterms == MAX_XOR_TERMS) return false;
+        g = xp->nterms++;
+        xp->grouped[g] = 0;
+        xp->shift[g] = 0;
+        xp->cm[g] = t.cm;
+        xp->tbit[g] = t.flip;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Double pair passes. A float-pair pair block costs about as much arithmetic as its pass takes
+// to stream the register, so two blocks on disjoint bit pairs share one pass (k_pair2: 16
+// amplitudes per thread). Consecutive pair passes on pairwise disjoint bits commute and are
+// matched two by two; an XOR pass next to such a run (the CNot layer between two brickwork
+// layers) is split into its terms, and every term whose bits lie inside a matched tile becomes a
+// register permutation of that tile: applied before the blocks when the XOR pass precedes the
+// run, after them when it follows. The matching prefers tiles that take terms of the preceding
+// XOR pass (they cannot wait), then tiles that take terms of the following one; terms no tile
+// takes stay in a smaller XOR pass at the original position.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+uint64_t xterm_bits(const XTerm& t) { return t.cm | t.flip; }
+
+double xor_touched(const std::vector<XTerm>& ts) {
+    double touched = 0.0;
+    for (const XTerm& t : ts) touched += t.swap ? 0.5 : std::ldexp(1.0, -popcount64(t.cm));
+    return std::min(1.0, touched);
+}
+
+bool push_xor_pass(const std::vector<XTerm>& ts, std::vector<Pass>& out) {
+    if (ts.empty()) return true;
+    Pass x;
+    x.xor_pass = true;
+    if (!xor_from_terms(ts, &x.xp)) return false;
+    x.touched = xor_touched(ts);
+    out.push_back(x);
+    return true;
+}
+
+uint64_t pass_pair_bits(const Pass& p) { return (1ull << p.bits[0]) | (1ull << p.bits[1]); }
+
+bool is_single_pair(const Pass& p) { return p.pair >= 0 && p.pair2 < 0; }
+
+}  // namespace
+
+void group_pair_passes(Plan* plan) {
+    const std::vector<Pass> in = plan->passes;
+    std::vector<Pass> out;
+    std::vector<XTerm> pending;  // terms of the XOR pass just before the current run
+    size_t i = 0;
+    while (i < in.size()) {
+        if (!is_single_pair(in[i])) {
+            if (in[i].xor_pass && i + 1 < in.size() && is_single_pair(in[i + 1])) {
+                pending = xor_terms(in[i].xp);  // placed by the run that follows
+            } else {
+                out.push_back(in[i]);
+            }
+            ++i;
+            continue;
+        }
+        // the run: pair passes on pairwise disjoint bits
+        size_t j = i;
+        uint64_t used = 0;
+        while (j < in.size() && is_single_pair(in[j]) && !(pass_pair_bits(in[j]) & used)) {
+            used |= pass_pair_bits(in[j]);
+            ++j;
+        }
+        const size_t m = j - i;
+        std::vector<XTerm> next;
+        const bool next_xor = j < in.size() && in[j].xor_pass;
+        if (next_xor) next = xor_terms(in[j].xp);
+        // greedy matching: heaviest tiles first (4 per preceding-XOR term, 1 per following)
+        std::vector<int> mate(m, -1);
+        struct Edge {
+            int w, a, b;
+        };
+        std::vector<Edge> edges;
+        if (m <= 64) {
+            for (size_t a = 0; a < m; ++a)
+                for (size_t b = a + 1; b < m; ++b) {
+                    const uint64_t mask = pass_pair_bits(in[i + a]) | pass_pair_bits(in[i + b]);
+                    int w = 0;
+                    for (const XTerm& t : pending) w += (xterm_bits(t) & ~mask) ? 0 : 4;
+                    for (const XTerm& t : next) w += (xterm_bits(t) & ~mask) ? 0 : 1;
+                    if (w > 0) edges.push_back(Edge{w, (int)a, (int)b});
+                }
+            std::stable_sort(edges.begin(), edges.end(),
+                             [](const Edge& x, const Edge& y) { return x.w > y.w; });
+            for (const Edge& e : edges)
+                if (mate[e.a] < 0 && mate[e.b] < 0) {
+                    mate[e.a] = e.b;
+                    mate[e.b] = e.a;
+                }
+        }
+        for (size_t a = 0; a < m; ++a) {  // the rest two by two in order
+            if (mate[a] >= 0) continue;
+            for (size_t b = a + 1; b < m; ++b)
+                if (mate[b] < 0) {
+                    mate[a] = (int)b;
+                    mate[b] = (int)a;
+                    break;
+                }
+        }
+        std::vector<Pass> groups;
+        for (size_t a = 0; a < m; ++a) {
+            if (mate[a] >= 0 && mate[a] < (int)a) continue;
+            if (mate[a] < 0) {
+                groups.push_back(in[i + a]);
+                continue;
+            }
+            const Pass& pa = in[i + a];
+            const Pass& pb = in[i + mate[a]];
+            Pass g;
+            int bits[4] = {pa.bits[0], pa.bits[1], pb.bits[0], pb.bits[1]};
+            std::sort(bits, bits + 4);
+            g.nbits = 4;
+            for (int q = 0; q < 4; ++q) g.bits[q] = bits[q];
+            g.arith = true;
+            g.cost = pa.cost + pb.cost;
+            g.touched = 1.0;
+            g.pair = pa.pair;
+            g.pair2 = pb.pair;
+            groups.push_back(g);
+        }
+        auto place = [&](std::vector<XTerm>& terms, bool before) {
+            std::vector<XTerm> rest;
+            for (const XTerm& t : terms) {
+                bool placed = false;
+                for (Pass& g : groups) {
+                    if (g.pair2 < 0) continue;
+                    uint64_t mask = 0;
+                    for (int q = 0; q < 4; ++q) mask |= 1ull << g.bits[q];
+                    std::vector<XTerm>& dst = before ? g.pre : g.post;
+                    if ((xterm_bits(t) & ~mask) == 0 && (int)dst.size() < MAX_TILE_XTERMS) {
+                        dst.push_back(t);
+                        placed = true;
+                        break;
+                    }
+                }
+                if (!placed) rest.push_back(t);
+            }
+            terms.swap(rest);
+        };
+        place(pending, true);
+        if (!push_xor_pass(pending, out)) {  // cannot happen: a subset regroups into fewer entries
+            plan->passes = in;
+            return;
+        }
+        pending.clear();
+        place(next, false);
+        for (const Pass& g : groups) out.push_back(g);
+        if (next_xor) {
+            if (j + 1 < in.size() && is_single_pair(in[j + 1])) pending = next;
+            else if (!push_xor_pass(next, out)) {
+                plan->passes = in;
+                return;
+            }
+            ++j;
+        }
+        i = j;
+    }
+    if (!pending.empty() && !push_xor_pass(pending, out)) {
+        plan->passes = in;
+        return;
+    }
+    plan->passes.swap(out);
+}
+
 DevStep dense_step(cd u00, cd u01, cd u10, cd u11) {
     DevStep s = blank_step(ST_DENSE);
     set_entry(s, 0, u00);
@@ -1024,6 +1249,7 @@ int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size
         cur_steps.push_back(h);
     }
     flush();
+    if (opt.pair_fusion && opt.group_pairs) group_pair_passes(plan);
     return QGPU_OK;
 }
 

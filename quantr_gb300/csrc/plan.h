@@ -84,9 +84,18 @@ struct XorPerm {
     int grouped[MAX_XOR_TERMS];
 };
 
+// One term of an XOR run: a controlled X (flip = its target bit, applied where (i & cm) == cm)
+// or a swap (swap = true, cm = flip = its two bits, applied where exactly one of them is set).
+struct XTerm {
+    uint64_t cm = 0, flip = 0;
+    bool swap = false;
+};
+constexpr int MAX_PASS_BITS = 4;       // widest pass: two pair blocks on four bits
+constexpr int MAX_TILE_XTERMS = 8;     // XOR terms a double pair pass applies before / after
+
 struct Pass {
     int nbits = 0;                     // tile bits
-    int bits[MAX_TILE_BITS];           // full-index bit positions, ascending
+    int bits[MAX_PASS_BITS];           // full-index bit positions, ascending
     bool xor_pass = false;             // the pass is one XorPerm (k_xor_perm)
     XorPerm xp;
     bool arith = false;                // needs float-pair / f64 arithmetic
@@ -95,6 +104,11 @@ struct Pass {
     std::vector<DevStep> steps;
     int custom = -1;                   // >= 0: this pass is a Custom gate (group kernel)
     int pair = -1;                     // >= 0: this pass is pair block `pair` (k_pair kernel)
+    // >= 0: a double pair pass (k_pair2): blocks `pair` and `pair2` on disjoint bit pairs of the
+    // four tile bits, with the XOR terms `pre` applied before them and `post` after them (every
+    // term's bits lie in the tile, so each thread permutes only its own 16 amplitudes)
+    int pair2 = -1;
+    std::vector<XTerm> pre, post;
 };
 
 // A 4x4 block over full-index bits hi > lo, local index l = 2 * bit(hi) + bit(lo).
@@ -126,7 +140,13 @@ struct PlanOptions {
     bool xor_runs = true;              // runs of >= 3 commuting controlled-X gates -> one pass
     bool pair_fusion = false;          // fuse gates on two wires into 4x4 blocks where cheaper
     int table_bits = 10;               // width of a phase-table field (<= MAX_TABLE_BITS)
+    bool group_pairs = true;           // with pair_fusion: two pair blocks per pass, XOR terms folded in
 };
+
+// Elementary terms of an XOR pass, and the pass rebuilt from a subset of them (false when the
+// terms need more than MAX_XOR_TERMS entries).
+std::vector<XTerm> xor_terms(const XorPerm& xp);
+bool xor_from_terms(const std::vector<XTerm>& ts, XorPerm* xp);
 
 int build_plan(const qgpu_op* ops, size_t n_ops, int n, const double* mats, size_t n_mats,
                const uint8_t* none, size_t n_none, const PlanOptions& opt, Plan* plan);

@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "internal.cuh"
@@ -932,7 +933,7 @@ struct BitPermArgs {
 
 template <class S>
 __global__ void __launch_bounds__(256) k_bitperm(S* __restrict__ st, const __grid_constant__ BitPermArgs p) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     const int T = 1 << p.nb;
     S* tA = reinterpret_cast<S*>(smem);
     S* tB = tA + T;
@@ -1199,6 +1200,211 @@ static int launch_pair(qgpu_handle* h, const PairBlock& pb, bool resident) {
     return QGPU_OK;
 }
 
+// ---- double pair passes: two 4x4 blocks on disjoint bit pairs of a 4-bit tile --------------
+// Each thread owns one tile of 16 amplitudes (full indices base | combinations of the 4 bits),
+// gathers them through the `pre` XOR terms, applies block A (the one on local bit 0) and block B,
+// and scatters them through the `post` terms. Every term flips only tile bits, so sources and
+// destinations are the thread's own 16 slots and the pass stays in place.
+struct Pair2Params {
+    uint64_t ngroups;                   // dim / 16
+    int bits[4];                        // full-index bits, ascending
+    // full-index offset, within the tile, that local slot j is read from / written to: the
+    // identity, or the permutation of the XOR terms folded before / after the blocks (their bits
+    // all lie in the tile, so the permutation is the same for every tile)
+    uint64_t pre_off[16], post_off[16];
+};
+struct Pair2ParamsFF : Pair2Params {
+    uint64_t pka[128], pkb[128];        // PairBlock::pk of blocks A and B
+};
+struct Pair2Params32 : Pair2Params {
+    float2 ma[4][4], mb[4][4];          // m[out][in] of blocks A and B
+};
+
+// PART: which local bits block A holds with local bit 0 (0: bit 1, 1: bit 2, 2: bit 3); block B
+// holds the other two.
+template <int PART>
+struct Pair2Layout {
+    static constexpr int A0 = 0, A1 = PART + 1;
+    static constexpr int B0 = PART == 0 ? 2 : 1, B1 = PART == 2 ? 2 : 3;
+};
+
+// Four lanes share a tile: lane `sub` first holds the quad over block A's bits at B-combination
+// sub (four loads), applies A, and the tile is transposed through shared memory so that it then
+// holds the quad over block B's bits at A-combination sub; it applies B and stores. A thread so
+// keeps one quad in registers, like k_pair. Shared layout per tile: 20 16-byte units (4 of
+// padding), element (a, b) at unit 4a + (b ^ a): the stores of one a and the loads of one b both
+// hit eight distinct bank groups per quarter warp.
+constexpr int PAIR2_THREADS = 256;
+constexpr int PAIR2_UNITS = 20;
+
+template <class P, int PART, class Prm, class Apply>
+__device__ __forceinline__ void pair2_body(typename P::S* __restrict__ st, const Prm& p,
+                                           Apply&& apply) {
+    using L = Pair2Layout<PART>;
+    using R = typename P::R;
+    __shared__ R xs[PAIR2_THREADS / 4][PAIR2_UNITS];
+    const int sub = threadIdx.x & 3;
+    const int tl = threadIdx.x >> 2;
+    // local slot of A-combination a and B-combination b
+    auto slot = [](int a, int b) {
+        return ((a & 1) << L::A0) | ((a >> 1) << L::A1) | ((b & 1) << L::B0) | ((b >> 1) << L::B1);
+    };
+    const uint64_t tiles_per_cta = PAIR2_THREADS / 4;
+    const uint64_t tstride = (uint64_t)gridDim.x * tiles_per_cta;
+    // every warp runs the same number of iterations (shared-memory exchange inside)
+    const uint64_t wfirst = blockIdx.x * tiles_per_cta + (tl & ~7);
+    for (uint64_t g0 = wfirst; g0 < p.ngroups; g0 += tstride) {
+        const uint64_t g = g0 + (tl & 7);
+        const bool active = g < p.ngroups;
+        const uint64_t base =
+            insert_zero(insert_zero(insert_zero(insert_zero(active ? g : g0, p.bits[0]), p.bits[1]),
+                                    p.bits[2]),
+                        p.bits[3]);
+        R w[4];
+        // the slot offsets are re-read from the parameter bank every iteration (hoisted out of
+        // the loop they would take 16 registers and spill under the 64-register bound)
+        int ls;
+        asm volatile("mov.b32 %0, %1;" : "=r"(ls) : "r"(sub));
+        if (active) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a) w[a] = P::load(st[base | p.pre_off[slot(a, ls)]]);
+            apply(w, 0);
+#pragma unroll
+            for (int a = 0; a < 4; ++a) xs[tl][4 * a + (sub ^ a)] = w[a];
+        }
+        __syncwarp();
+        if (active) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b) w[b] = xs[tl][4 * sub + (b ^ sub)];
+        }
+        __syncwarp();
+        if (active) {
+            apply(w, 1);
+#pragma unroll
+            for (int b = 0; b < 4; ++b) st[base | p.post_off[slot(ls, b)]] = P::store(w[b]);
+        }
+    }
+}
+
+template <class P, int PART>
+// 64 registers on the resident layout (4 CTAs per SM; unbounded, the compiler keeps block
+// constants in registers across tiles, about 100 registers and 2 CTAs per SM); 80 with the
+// split and join of the plain layout.
+__global__ void __launch_bounds__(PAIR2_THREADS, std::is_same<P, PolFFR>::value ? 4 : 3) k_pair2(typename P::S* __restrict__ st,
+                                                  const __grid_constant__ Pair2ParamsFF p) {
+    pair2_body<P, PART>(st, p, [&](ffp w[4], int blk) { ff_pair(w, blk ? p.pkb : p.pka); });
+}
+
+struct PolPlainF32 {
+    using S = float2;
+    using R = float2;
+    static __device__ __forceinline__ R load(S a) { return a; }
+    static __device__ __forceinline__ S store(R a) { return a; }
+};
+
+__device__ __forceinline__ void f32_pair(float2 x[4], const float2 (*m)[4]) {
+    float2 y[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const float2 u = m[r][c];
+            re = fmaf(u.x, x[c].x, fmaf(-u.y, x[c].y, re));
+            im = fmaf(u.x, x[c].y, fmaf(u.y, x[c].x, im));
+        }
+        y[r] = make_float2(re, im);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) x[r] = y[r];
+}
+
+template <int PART>
+__global__ void __launch_bounds__(PAIR2_THREADS) k_pair2_f32(float2* __restrict__ st,
+                                                   const __grid_constant__ Pair2Params32 p) {
+    pair2_body<PolPlainF32, PART>(st, p,
+                                  [&](float2 w[4], int blk) { f32_pair(w, blk ? p.mb : p.ma); });
+}
+
+// Offsets of the 16 tile slots after the permutation i -> i ^ f(i) of XOR terms whose bits all
+// lie in the tile (the permutation does not depend on the tile's base).
+static void slot_offsets(const int bits[4], const std::vector<XTerm>& ts, uint64_t off[16]) {
+    for (int j = 0; j < 16; ++j) {
+        uint64_t i = 0;
+        for (int m = 0; m < 4; ++m)
+            if ((j >> m) & 1) i |= 1ull << bits[m];
+        uint64_t f = 0;
+        for (const XTerm& t : ts) {
+            const uint64_t c = i & t.cm;
+            if (t.swap ? (c != 0 && c != t.cm) : (c == t.cm)) f |= t.flip;
+        }
+        off[j] = i ^ f;
+    }
+}
+
+static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, bool resident) {
+    // block A holds local bit 0 (the lowest tile bit)
+    const PairBlock* a = &plan.pairs[ps.pair];
+    const PairBlock* b = &plan.pairs[ps.pair2];
+    if (b->lo == ps.bits[0]) std::swap(a, b);
+    int part = -1;
+    for (int q = 1; q < 4; ++q)
+        if (a->hi == ps.bits[q]) part = q - 1;
+    uint64_t tile = 0;
+    for (int m = 0; m < 4; ++m) tile |= 1ull << ps.bits[m];
+    bool inside = true;
+    for (const auto* ts : {&ps.pre, &ps.post})
+        for (const XTerm& t : *ts) inside = inside && ((t.cm | t.flip) & ~tile) == 0;
+    if (a->lo != ps.bits[0] || part < 0 || !inside)
+        return fail(QGPU_ERR_UNSUPPORTED, "double pair pass: blocks or terms outside the tile");
+    auto fill = [&](Pair2Params& q) {
+        std::memset(&q, 0, sizeof(Pair2Params));
+        q.ngroups = h->dim >> 4;
+        for (int m = 0; m < 4; ++m) q.bits[m] = ps.bits[m];
+        slot_offsets(ps.bits, ps.pre, q.pre_off);
+        slot_offsets(ps.bits, ps.post, q.post_off);
+    };
+    // four threads per 16-amplitude tile
+    uint64_t blocks = std::max<uint64_t>(
+        1, std::min<uint64_t>(((h->dim >> 4) + PAIR2_THREADS / 4 - 1) / (PAIR2_THREADS / 4),
+                              (uint64_t)h->sm_count * 8));
+    if (h->precision == QGPU_C64) {
+        Pair2Params32 q;
+        fill(q);
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) {
+                q.ma[r][c] = make_float2((float)a->m[r][c].real(), (float)a->m[r][c].imag());
+                q.mb[r][c] = make_float2((float)b->m[r][c].real(), (float)b->m[r][c].imag());
+            }
+        float2* s = (float2*)cur_state(h);
+        if (part == 0) k_pair2_f32<0><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+        else if (part == 1) k_pair2_f32<1><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+        else k_pair2_f32<2><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+        QGPU_CHECK_LAUNCH("k_pair2_f32");
+        h->launches++;
+        h->h2d_bytes += sizeof(q);
+        return QGPU_OK;
+    }
+    Pair2ParamsFF q;
+    fill(q);
+    std::memcpy(q.pka, a->pk, sizeof(q.pka));
+    std::memcpy(q.pkb, b->pk, sizeof(q.pkb));
+    double2* s = (double2*)cur_state(h);
+    if (resident) {
+        if (part == 0) k_pair2<PolFFR, 0><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+        else if (part == 1) k_pair2<PolFFR, 1><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+        else k_pair2<PolFFR, 2><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+    } else {
+        if (part == 0) k_pair2<PolFF, 0><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+        else if (part == 1) k_pair2<PolFF, 1><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+        else k_pair2<PolFF, 2><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+    }
+    QGPU_CHECK_LAUNCH("k_pair2");
+    h->launches++;
+    h->h2d_bytes += sizeof(q);
+    return QGPU_OK;
+}
+
 // Whether a float-pair plan runs on the resident layout: it saves the split and join of every
 // arithmetic pass for two extra streaming passes, so it pays once the plan carries several
 // arithmetic passes. Custom blocks read complex128 and keep the plan on the plain layout.
@@ -1275,6 +1481,10 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
             QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + li)], h->stream));
             if (!ps) {
                 prof_names.push_back("k_ff_layout");
+            } else if (ps->pair2 >= 0) {
+                prof_names.push_back(h->precision == QGPU_C64 ? "k_pair2<f32>"
+                                     : resident               ? "k_pair2<ffr>"
+                                                              : "k_pair2<ff>");
             } else if (ps->pair >= 0) {
                 prof_names.push_back(h->precision == QGPU_C64 ? "k_pair<f32>"
                                      : resident               ? "k_pair<ffr>"
@@ -1293,6 +1503,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
         int st = QGPU_OK;
         if (!ps) {
             st = launch_ff_layout(h, first_conv);
+        } else if (ps->pair2 >= 0) {
+            st = launch_pair2(h, plan, *ps, resident);
         } else if (ps->pair >= 0) {
             st = launch_pair(h, plan.pairs[ps->pair], resident);
         } else if (ps->custom >= 0) {
@@ -1368,6 +1580,8 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     o.max_arith_bits = o.policy == POL_FF ? env_int("QGPU_ARITH_TILE_BITS", 2) : MAX_TILE_BITS;
     // 4x4 pair blocks (k_pair) for the float-pair policy; QGPU_PAIR_FUSION=0 turns them off
     o.pair_fusion = (o.policy == POL_FF || o.policy == POL_F32) && env_int("QGPU_PAIR_FUSION", 1) != 0;
+    // two pair blocks per pass with the XOR layers folded in (k_pair2); QGPU_PAIR_GROUP=0: off
+    o.group_pairs = env_int("QGPU_PAIR_GROUP", 1) != 0;
     // phase-table field width (tuning knob QGPU_TABLE_BITS): 10 bits measured best on GB300 for
     // the 30-qubit QFT rows (1114 ms per step; 11: 1118, 12: 1156, 9: 1182 ms)
     o.table_bits = env_int("QGPU_TABLE_BITS", 10);

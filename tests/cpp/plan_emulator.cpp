@@ -124,7 +124,7 @@ static void apply_step(const qgpu::DevStep& s, const qgpu::Pass& p, const qgpu::
 
 int main(int argc, char** argv) {
     if (argc < 6) {
-        std::fprintf(stderr, "usage: %s n ops mats none out [pair budget arith_bits]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s n ops mats none out [pair budget arith_bits plan_only group]\n", argv[0]);
         return 2;
     }
     const int n = std::atoi(argv[1]);
@@ -136,23 +136,74 @@ int main(int argc, char** argv) {
     opt.pair_fusion = argc > 6 ? std::atoi(argv[6]) != 0 : true;
     opt.budget = argc > 7 ? std::atoi(argv[7]) : 280;
     opt.max_arith_bits = argc > 8 ? std::atoi(argv[8]) : 2;
+    opt.group_pairs = argc > 10 ? std::atoi(argv[10]) != 0 : true;
     qgpu::Plan plan;
     if (qgpu::build_plan(ops.data(), ops.size(), n, mats.data(), mats.size(), none.data(),
                          none.size(), opt, &plan) != QGPU_OK)
         return 1;
     if (argc > 9 && std::atoi(argv[9]) != 0) {  // plan only: report the pass counts
-        int counts[3] = {0, 0, 0};
-        for (const qgpu::Pass& p : plan.passes)
-            ++counts[p.pair >= 0 ? 0 : (p.xor_pass ? 2 : 1)];
-        std::printf("passes %zu pair %d tile %d xor %d\n", plan.passes.size(), counts[0], counts[1],
-                    counts[2]);
+        int counts[4] = {0, 0, 0, 0};
+        size_t folded = 0;
+        for (const qgpu::Pass& p : plan.passes) {
+            ++counts[p.pair2 >= 0 ? 3 : (p.pair >= 0 ? 0 : (p.xor_pass ? 2 : 1))];
+            folded += p.pre.size() + p.post.size();
+        }
+        std::printf("passes %zu pair %d tile %d xor %d pair2 %d folded %zu\n", plan.passes.size(),
+                    counts[0], counts[1], counts[2], counts[3], folded);
         return 0;
     }
     const uint64_t dim = 1ull << n;
     std::vector<cd> st(dim);
     st[0] = 1.0;
-    int npair = 0, ntile = 0, nxor = 0;
+    int npair = 0, ntile = 0, nxor = 0, npair2 = 0;
+    size_t nfolded = 0;
+    // a 4x4 block on bits (hi, lo), local index 2 * bit(hi) + bit(lo)
+    auto apply_block = [&](const qgpu::PairBlock& pb) {
+        for (uint64_t g = 0; g < (dim >> 2); ++g) {
+            const uint64_t b = insert_zero(insert_zero(g, pb.lo), pb.hi);
+            const uint64_t idx[4] = {b, b | (1ull << pb.lo), b | (1ull << pb.hi),
+                                     b | (1ull << pb.lo) | (1ull << pb.hi)};
+            cd x[4], y[4];
+            for (int j = 0; j < 4; ++j) x[j] = st[idx[j]];
+            for (int r = 0; r < 4; ++r) {
+                y[r] = 0.0;
+                for (int c = 0; c < 4; ++c) y[r] += pb.m[r][c] * x[c];
+            }
+            for (int j = 0; j < 4; ++j) st[idx[j]] = y[j];
+        }
+    };
+    // i -> i ^ f(i) for XOR terms (each an involution; the terms commute)
+    auto apply_terms = [&](const std::vector<qgpu::XTerm>& ts) {
+        if (ts.empty()) return;
+        std::vector<cd> nx(dim);
+        for (uint64_t i = 0; i < dim; ++i) {
+            uint64_t f = 0;
+            for (const qgpu::XTerm& t : ts) {
+                const uint64_t c = i & t.cm;
+                if (t.swap ? (c != 0 && c != t.cm) : (c == t.cm)) f |= t.flip;
+            }
+            nx[i] = st[i ^ f];
+        }
+        st.swap(nx);
+    };
     for (const qgpu::Pass& p : plan.passes) {
+        if (p.pair2 >= 0) {
+            ++npair2;
+            nfolded += p.pre.size() + p.post.size();
+            uint64_t mask = 0;
+            for (int m = 0; m < p.nbits; ++m) mask |= 1ull << p.bits[m];
+            for (const auto* ts : {&p.pre, &p.post})
+                for (const qgpu::XTerm& t : *ts)
+                    if ((t.cm | t.flip) & ~mask) {
+                        std::fprintf(stderr, "folded XOR term outside its tile\n");
+                        return 5;
+                    }
+            apply_terms(p.pre);
+            apply_block(plan.pairs[p.pair]);
+            apply_block(plan.pairs[p.pair2]);
+            apply_terms(p.post);
+            continue;
+        }
         if (p.custom >= 0) {
             std::fprintf(stderr, "custom passes are not emulated\n");
             return 4;
@@ -214,6 +265,7 @@ int main(int argc, char** argv) {
     }
     std::ofstream out(argv[5], std::ios::binary);
     out.write(reinterpret_cast<const char*>(st.data()), (std::streamsize)(dim * sizeof(cd)));
-    std::printf("passes %zu pair %d tile %d xor %d\n", plan.passes.size(), npair, ntile, nxor);
+    std::printf("passes %zu pair %d tile %d xor %d pair2 %d folded %zu\n", plan.passes.size(), npair,
+                ntile, nxor, npair2, nfolded);
     return 0;
 }

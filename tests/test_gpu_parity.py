@@ -159,6 +159,43 @@ def test_commuting_cx_runs(oracle, precision):
 
 
 @pytest.mark.parametrize("precision", [nat.QGPU_C128, nat.QGPU_C64])
+@pytest.mark.parametrize("n", [8, 13])
+def test_double_pair_passes_folded_xor_terms(oracle, precision, n):
+    """Pair blocks two per pass (k_pair2) with the XOR layers between them folded in as tile
+    permutations before and after the blocks: CNots across neighbouring blocks, CNots inside a
+    block's wires, swaps across two blocks, and a Toffoli spanning two tiles (left in an XOR
+    pass); random register, so every slot of a tile carries a distinct value."""
+    rng = np.random.default_rng(40 + n)
+    reg = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    reg /= np.linalg.norm(reg)
+    b = ProgramBuilder(n)
+    for layer in range(6):
+        for w in range(n):
+            b.add("Ry", w, (), param=float(rng.uniform(0, 6.3)))
+            b.add("Rz", w, (), param=float(rng.uniform(0, 6.3)))
+        for w in range(0, n - 1, 2):
+            b.add("CNot", w + 1, (w,))
+        for w in range(n):
+            b.add("Rx", w, (), param=float(rng.uniform(0, 6.3)))
+        if layer % 2 == 0:
+            for w in range(1, n - 2, 2):
+                b.add("CNot", w + 1, (w,))
+            b.add("Toffoli", 7, (0, 3))
+        else:
+            b.add("Swap", 2, (5,))
+            b.add("CNot", 1, (0,))
+            b.add("CNot", 4, (3,))
+            b.add("CNot", 7, (6,))
+    prog = b.build()
+    if precision == nat.QGPU_C64:
+        reg = reg.astype(np.complex64).astype(np.complex128)
+    ref = oracle.simulate(prog, reg, engine=oracle.DENSE)
+    out = run_gpu(prog, "fast", precision=precision, reg=reg)
+    tol = TOL_FAST if precision == nat.QGPU_C128 else 1e-5
+    assert np.max(np.abs(out - ref)) <= tol
+
+
+@pytest.mark.parametrize("precision", [nat.QGPU_C128, nat.QGPU_C64])
 @pytest.mark.parametrize("n,pairs", [
     (12, [(i, 11 - i) for i in range(6)]),          # full bit reversal, even width
     (13, [(i, 12 - i) for i in range(6)]),          # odd width: middle wire stays

@@ -29,30 +29,72 @@ def emulator(tmp_path_factory):
     return exe
 
 
-def run_plan(emulator, prog, tmp_path, pair=1, budget=280, arith_bits=2):
+def run_plan(emulator, prog, tmp_path, pair=1, budget=280, arith_bits=2, group=1):
     f = {k: tmp_path / f"{k}.bin" for k in ("ops", "mats", "none", "out")}
     np.ascontiguousarray(prog.ops).tofile(f["ops"])
     np.ascontiguousarray(prog.mats, dtype=np.float64).tofile(f["mats"])
     np.ascontiguousarray(prog.none, dtype=np.uint8).tofile(f["none"])
     r = subprocess.run([str(emulator), str(prog.n), str(f["ops"]), str(f["mats"]), str(f["none"]),
-                        str(f["out"]), str(pair), str(budget), str(arith_bits)],
+                        str(f["out"]), str(pair), str(budget), str(arith_bits), "0", str(group)],
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     counts = dict(zip(r.stdout.split()[::2], map(int, r.stdout.split()[1::2])))
     return np.fromfile(f["out"], dtype=np.complex128), counts
 
 
+@pytest.mark.parametrize("group", [0, 1])
 @pytest.mark.parametrize("pair", [0, 1])
 @pytest.mark.parametrize("budget", [140, 280])
-@pytest.mark.parametrize("n", [6, 11])
-def test_brickwork_qft_plan(emulator, oracle, tmp_path, n, budget, pair):
+@pytest.mark.parametrize("n", [6, 10, 11])
+def test_brickwork_qft_plan(emulator, oracle, tmp_path, n, budget, pair, group):
     prog = W.brickwork_qft(n=n, layers=20, seed=2)
-    out, counts = run_plan(emulator, prog, tmp_path, pair, budget)
+    out, counts = run_plan(emulator, prog, tmp_path, pair, budget, group=group)
     ref = oracle.simulate(prog, engine=oracle.DENSE)
     assert np.max(np.abs(out - ref)) <= TOL
     if pair:
         # two layers of a wire pair and their CNot per block
-        assert counts["pair"] >= 10 * (n // 2) - n
+        assert counts["pair"] + 2 * counts["pair2"] >= 10 * (n // 2) - n
+    if pair and group and n % 2 == 0 and n // 2 - 1 >= 3:
+        # blocks run two per pass; the CNot layers between brickwork layers (XOR passes of
+        # n/2 - 1 terms) are folded into the double passes as register permutations, all but
+        # the last layer's leftovers
+        assert counts["pair2"] >= 10 * ((n // 2) // 2)
+        assert counts["folded"] >= 9 * (n // 2 - 1)
+        assert counts["xor"] <= 2
+
+
+def test_double_pair_passes_fold_xor_terms(emulator, oracle, tmp_path):
+    """Double pair passes with XOR terms folded before and after the blocks: CNots between and
+    inside the tiles, swaps across two blocks, and a Toffoli whose bits span two tiles (left in
+    an XOR pass)."""
+    n = 8
+    rng = np.random.default_rng(11)
+    b = ProgramBuilder(n)
+    for layer in range(8):
+        for w in range(n):
+            b.add("Ry", w, (), param=float(rng.uniform(0, 6.3)))
+            b.add("Rz", w, (), param=float(rng.uniform(0, 6.3)))
+        for w in range(0, n, 2):
+            b.add("CNot", w + 1, (w,))
+        for w in range(n):
+            b.add("Rx", w, (), param=float(rng.uniform(0, 6.3)))
+        if layer % 2 == 0:
+            b.add("CNot", 2, (1,))
+            b.add("CNot", 4, (3,))
+            b.add("CNot", 6, (5,))
+            b.add("Toffoli", 7, (0, 3))
+        else:
+            b.add("Swap", 2, (5,))
+            b.add("CNot", 1, (0,))
+            b.add("CNot", 4, (3,))
+            b.add("CNot", 7, (6,))
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    for group in (0, 1):
+        out, counts = run_plan(emulator, prog, tmp_path, 1, group=group)
+        assert np.max(np.abs(out - ref)) <= TOL
+        if group:
+            assert counts["pair2"] > 0 and counts["folded"] > 0
 
 
 @pytest.mark.parametrize("seed", [1, 11, 12])
@@ -119,6 +161,7 @@ def test_pair_blocks_interleaved_wires(emulator, oracle, tmp_path):
         b.add("Swap", 2, (5,))
     prog = b.build()
     ref = oracle.simulate(prog, engine=oracle.DENSE)
-    out, counts = run_plan(emulator, prog, tmp_path, 1)
-    assert counts["pair"] > 0
-    assert np.max(np.abs(out - ref)) <= TOL
+    for group in (0, 1):
+        out, counts = run_plan(emulator, prog, tmp_path, 1, group=group)
+        assert counts["pair"] + counts["pair2"] > 0
+        assert np.max(np.abs(out - ref)) <= TOL
