@@ -141,6 +141,35 @@ int main(int argc, char** argv) {
     if (qgpu::build_plan(ops.data(), ops.size(), n, mats.data(), mats.size(), none.data(),
                          none.size(), opt, &plan) != QGPU_OK)
         return 1;
+    if (argc > 9 && std::atoi(argv[9]) == 2) {  // plan listing: one line per pass
+        for (const qgpu::Pass& p : plan.passes) {
+            if (p.pair2 >= 0) {
+                std::printf("pair2 bits %d %d %d %d pre %zu post %zu\n", p.bits[0], p.bits[1],
+                            p.bits[2], p.bits[3], p.pre.size(), p.post.size());
+            } else if (p.pair >= 0) {
+                std::printf("pair bits %d %d\n", p.bits[0], p.bits[1]);
+            } else if (p.xor_pass) {
+                std::printf("xor terms %d\n", p.xp.nterms);
+            } else if (p.custom >= 0) {
+                std::printf("custom\n");
+            } else {
+                std::printf("tile bits");
+                for (int m = 0; m < p.nbits; ++m) std::printf(" %d", p.bits[m]);
+                std::printf(" cost %d steps", p.cost);
+                for (const qgpu::DevStep& d : p.steps) {
+                    std::printf(" %d", d.type);
+                    if (d.type == qgpu::ST_TABLE) {
+                        std::printf("[");
+                        for (int f = 0; f < d.nfields; ++f)
+                            std::printf("%s%d+%d", f ? "," : "", d.tab_shift[f], d.tab_width[f]);
+                        std::printf(" cm %llx]", (unsigned long long)d.cm);
+                    }
+                }
+                std::printf("\n");
+            }
+        }
+        return 0;
+    }
     if (argc > 9 && std::atoi(argv[9]) != 0) {  // plan only: report the pass counts
         int counts[4] = {0, 0, 0, 0};
         size_t folded = 0;
