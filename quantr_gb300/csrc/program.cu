@@ -384,6 +384,16 @@ struct PolFFR : PolFF {
     static __device__ __forceinline__ S store(const R& r) { return ffr_store(r); }
 };
 
+// The first and the last arithmetic pass of a resident plan convert the layout themselves
+// (instead of a separate streaming pass each way): PolFFIn reads complex128 and writes the
+// resident layout, PolFFOut reads the resident layout and writes complex128.
+struct PolFFIn : PolFF {
+    static __device__ __forceinline__ S store(const R& r) { return ffr_store(r); }
+};
+struct PolFFOut : PolFF {
+    static __device__ __forceinline__ R load(S a) { return ffr_load(a); }
+};
+
 // moves and +-1/+-i phases on the resident layout (a phase of i swaps and negates both halves)
 struct PolRawFFR {
     using S = double2;
@@ -1109,7 +1119,7 @@ static int env_int(const char* name, int dflt) {
     return std::atoi(v);
 }
 
-static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, bool resident,
+static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, int lay,
                        const float4* tab_ff, const double2* tab_f64, TileParams& tp);
 
 static int launch_ff_layout(qgpu_handle* h, bool to_pairs) {
@@ -1155,7 +1165,12 @@ __global__ void __launch_bounds__(256) k_pair_f32(float2* __restrict__ st,
     }
 }
 
-static int launch_pair(qgpu_handle* h, const PairBlock& pb, bool resident) {
+// Layout of a float-pair pass: LAY_PLAIN (complex128 in and out), LAY_RES (resident in and out),
+// LAY_IN (complex128 in, resident out), LAY_OUT (resident in, complex128 out).
+enum PassLayout { LAY_PLAIN = 0, LAY_RES = 1, LAY_IN = 2, LAY_OUT = 3 };
+
+static int launch_pair(qgpu_handle* h, const PairBlock& pb, int lay) {
+    const bool resident = lay == LAY_RES;
     if (h->precision == QGPU_C64) {
         PairParams32 q;
         q.ngroups = h->dim >> 2;
@@ -1183,13 +1198,17 @@ static int launch_pair(qgpu_handle* h, const PairBlock& pb, bool resident) {
     if (blocks < 1) blocks = 1;
     double2* s = (double2*)cur_state(h);
     static const int variant = env_int("QGPU_PAIR_VARIANT", 0);  // tuning knob: 0, 1 or 2
-    if (variant == 2) {
+    if (variant == 2 && (lay == LAY_RES || lay == LAY_PLAIN)) {
         blocks = std::max<uint64_t>(1, std::min<uint64_t>((p.ngroups + 511) / 512, cap));
         if (resident) k_pair<PolFFR, 2><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
         else k_pair<PolFF, 2><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
-    } else if (variant == 1) {
+    } else if (variant == 1 && (lay == LAY_RES || lay == LAY_PLAIN)) {
         if (resident) k_pair<PolFFR, 1><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
         else k_pair<PolFF, 1><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+    } else if (lay == LAY_IN) {
+        k_pair<PolFFIn, 0><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+    } else if (lay == LAY_OUT) {
+        k_pair<PolFFOut, 0><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
     } else {
         if (resident) k_pair<PolFFR, 0><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
         else k_pair<PolFF, 0><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
@@ -1342,7 +1361,15 @@ static void slot_offsets(const int bits[4], const std::vector<XTerm>& ts, uint64
     }
 }
 
-static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, bool resident) {
+template <class P>
+static void launch_pair2_pol(qgpu_handle* h, int part, uint64_t blocks, double2* s,
+                             const Pair2ParamsFF& q) {
+    if (part == 0) k_pair2<P, 0><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+    else if (part == 1) k_pair2<P, 1><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+    else k_pair2<P, 2><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+}
+
+static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, int lay) {
     // block A holds local bit 0 (the lowest tile bit)
     const PairBlock* a = &plan.pairs[ps.pair];
     const PairBlock* b = &plan.pairs[ps.pair2];
@@ -1390,14 +1417,11 @@ static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, bool r
     std::memcpy(q.pka, a->pk, sizeof(q.pka));
     std::memcpy(q.pkb, b->pk, sizeof(q.pkb));
     double2* s = (double2*)cur_state(h);
-    if (resident) {
-        if (part == 0) k_pair2<PolFFR, 0><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
-        else if (part == 1) k_pair2<PolFFR, 1><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
-        else k_pair2<PolFFR, 2><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
-    } else {
-        if (part == 0) k_pair2<PolFF, 0><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
-        else if (part == 1) k_pair2<PolFF, 1><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
-        else k_pair2<PolFF, 2><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
+    switch (lay) {
+        case LAY_RES: launch_pair2_pol<PolFFR>(h, part, blocks, s, q); break;
+        case LAY_IN: launch_pair2_pol<PolFFIn>(h, part, blocks, s, q); break;
+        case LAY_OUT: launch_pair2_pol<PolFFOut>(h, part, blocks, s, q); break;
+        default: launch_pair2_pol<PolFF>(h, part, blocks, s, q); break;
     }
     QGPU_CHECK_LAUNCH("k_pair2");
     h->launches++;
@@ -1463,7 +1487,28 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
     TileParams tp;
     std::vector<std::string> prof_names;
     std::vector<double> prof_bytes;
-    const size_t nlaunch = plan.passes.size() + (convert ? 2 : 0);
+    // The first and the last arithmetic pass convert the layout themselves where they can: the
+    // first pass reads complex128, and the last one writes it when only slot permutations (XOR
+    // passes, layout-agnostic) follow. Otherwise a k_ff_layout pass converts.
+    int fuse_in = -1, fuse_out = -1;
+    if (convert && !plan.passes.empty()) {
+        auto fusable = [](const Pass& p) {
+            return p.custom < 0 && !p.xor_pass && (p.pair >= 0 || (p.arith && p.nbits <= MAX_TILE_BITS));
+        };
+        static const int fuse = env_int("QGPU_FUSE_LAYOUT", 1);  // tuning knob: 0 = separate passes
+        int last = (int)plan.passes.size() - 1;
+        while (last >= 0 && plan.passes[last].xor_pass) --last;
+        if (fuse && fusable(plan.passes[0])) fuse_in = 0;
+        if (fuse && last > 0 && fusable(plan.passes[last])) fuse_out = last;
+    }
+    const bool conv_first = convert && fuse_in < 0, conv_last = convert && fuse_out < 0;
+    auto layout_of = [&](int pi) {
+        if (!resident) return (int)LAY_PLAIN;
+        if (pi == fuse_in) return (int)LAY_IN;
+        if (pi == fuse_out) return (int)LAY_OUT;
+        return (int)LAY_RES;  // (passes after fuse_out are XOR passes: any layout)
+    };
+    const size_t nlaunch = plan.passes.size() + (conv_first ? 1 : 0) + (conv_last ? 1 : 0);
     size_t ev_base = 0;
     if (h->profile) {
         int st = prof_events(h, nlaunch, &ev_base);
@@ -1474,9 +1519,11 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
     const double full_bytes = 2.0 * (double)h->amp_bytes * (double)h->dim;
     for (size_t li = 0; li < nlaunch; ++li) {
         // launch li: [layout to pairs], passes..., [layout back]
-        const bool first_conv = convert && li == 0;
-        const bool last_conv = convert && li == nlaunch - 1;
-        const Pass* ps = (first_conv || last_conv) ? nullptr : &plan.passes[li - (convert ? 1 : 0)];
+        const bool first_conv = conv_first && li == 0;
+        const bool last_conv = conv_last && li == nlaunch - 1;
+        const int pi = (int)li - (conv_first ? 1 : 0);
+        const Pass* ps = (first_conv || last_conv) ? nullptr : &plan.passes[pi];
+        const int play = ps ? layout_of(pi) : LAY_PLAIN;  // this pass's layout
         if (h->profile) {
             QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + li)], h->stream));
             if (!ps) {
@@ -1504,15 +1551,15 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
         if (!ps) {
             st = launch_ff_layout(h, first_conv);
         } else if (ps->pair2 >= 0) {
-            st = launch_pair2(h, plan, *ps, resident);
+            st = launch_pair2(h, plan, *ps, play);
         } else if (ps->pair >= 0) {
-            st = launch_pair(h, plan.pairs[ps->pair], resident);
+            st = launch_pair(h, plan.pairs[ps->pair], play);
         } else if (ps->custom >= 0) {
             st = launch_group(h, gargs[ps->custom], (const uint8_t*)h->gates.ptr, lay[ps->custom]);
         } else if (ps->xor_pass) {
             st = launch_xor(h, ps->xp);
         } else {
-            st = launch_pass(h, *ps, pol, resident, tab_ff, tab_f64, tp);
+            st = launch_pass(h, *ps, pol, play, tab_ff, tab_f64, tp);
         }
         if (st != QGPU_OK) return st;
         if (h->profile) QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + li) + 1], h->stream));
@@ -1527,8 +1574,9 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
     return st;
 }
 
-static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, bool resident,
+static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, int lay,
                        const float4* tab_ff, const double2* tab_f64, TileParams& tp) {
+    const bool resident = lay == LAY_RES;
     {
         std::memset(&tp, 0, sizeof(tp));
         tp.nbits = ps.nbits;
@@ -1549,7 +1597,10 @@ static int launch_pass(qgpu_handle* h, const Pass& ps, int pol, bool resident,
         for (const DevStep& d : ps.steps) has_table = has_table || d.type == ST_TABLE;
         tp.streaming = streaming == 2 || (streaming == 1 && has_table);
         int st;
-        if (resident) {
+        if (lay == LAY_IN || lay == LAY_OUT) {
+            if (!ps.arith) return fail(QGPU_ERR_UNSUPPORTED, "layout-converting pass without arithmetic");
+            st = lay == LAY_IN ? launch_tile_k<PolFFIn>(h, tp) : launch_tile_k<PolFFOut>(h, tp);
+        } else if (resident) {
             st = ps.arith ? launch_tile_k<PolFFR>(h, tp) : launch_tile_k<PolRawFFR>(h, tp);
         } else if (!ps.arith) {
             st = (h->precision == QGPU_C64) ? launch_tile_k<PolRaw<float2>>(h, tp)
