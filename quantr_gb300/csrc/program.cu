@@ -1256,6 +1256,22 @@ struct Pair2Layout {
 constexpr int PAIR2_THREADS = 256;
 constexpr int PAIR2_UNITS = 20;
 
+// Applies fn(w[4]) to the four quads of v[16] over local bits (X0 < X1), quad order
+// l = 2 bit(X1) + bit(X0), for every combination of the other two local bits (Y0, Y1).
+template <int X0, int X1, int Y0, int Y1, class V, class F>
+__device__ __forceinline__ void tile_quads(V* v, F&& fn) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int jb = ((q & 1) << Y0) | ((q >> 1) << Y1);
+        V w[4] = {v[jb], v[jb | (1 << X0)], v[jb | (1 << X1)], v[jb | (1 << X0) | (1 << X1)]};
+        fn(w);
+        v[jb] = w[0];
+        v[jb | (1 << X0)] = w[1];
+        v[jb | (1 << X1)] = w[2];
+        v[jb | (1 << X0) | (1 << X1)] = w[3];
+    }
+}
+
 template <class P, int PART, class Prm, class Apply>
 __device__ __forceinline__ void pair2_body(typename P::S* __restrict__ st, const Prm& p,
                                            Apply&& apply) {
@@ -1339,10 +1355,25 @@ __device__ __forceinline__ void f32_pair(float2 x[4], const float2 (*m)[4]) {
 }
 
 template <int PART>
+// complex64: the pass is bound by HBM, not arithmetic, so one thread holds a whole tile (16
+// amplitudes, 32 registers) and a warp's load of one slot covers 32 consecutive tiles; the
+// blocks run on the tile's quads in registers.
 __global__ void __launch_bounds__(PAIR2_THREADS) k_pair2_f32(float2* __restrict__ st,
                                                    const __grid_constant__ Pair2Params32 p) {
-    pair2_body<PolPlainF32, PART>(st, p,
-                                  [&](float2 w[4], int blk) { f32_pair(w, blk ? p.mb : p.ma); });
+    using L = Pair2Layout<PART>;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < p.ngroups; g += stride) {
+        const uint64_t base =
+            insert_zero(insert_zero(insert_zero(insert_zero(g, p.bits[0]), p.bits[1]), p.bits[2]),
+                        p.bits[3]);
+        float2 v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = st[base | p.pre_off[j]];
+        tile_quads<L::A0, L::A1, L::B0, L::B1>(v, [&](float2 w[4]) { f32_pair(w, p.ma); });
+        tile_quads<L::B0, L::B1, L::A0, L::A1>(v, [&](float2 w[4]) { f32_pair(w, p.mb); });
+#pragma unroll
+        for (int j = 0; j < 16; ++j) st[base | p.post_off[j]] = v[j];
+    }
 }
 
 // Offsets of the 16 tile slots after the permutation i -> i ^ f(i) of XOR terms whose bits all
@@ -1404,6 +1435,9 @@ static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, int la
                 q.mb[r][c] = make_float2((float)b->m[r][c].real(), (float)b->m[r][c].imag());
             }
         float2* s = (float2*)cur_state(h);
+        blocks = std::max<uint64_t>(
+            1, std::min<uint64_t>((q.ngroups + PAIR2_THREADS - 1) / PAIR2_THREADS,
+                                  (uint64_t)h->sm_count * 8));
         if (part == 0) k_pair2_f32<0><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
         else if (part == 1) k_pair2_f32<1><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
         else k_pair2_f32<2><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
