@@ -84,6 +84,7 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.path = None
+        self._summary = None
 
     def __enter__(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -107,6 +108,12 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self) -> dict:
+        """Parses (once) and removes the sample file; later calls return the same summary."""
+        if self._summary is None:
+            self._summary = self._parse()
+        return self._summary
+
+    def _parse(self) -> dict:
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         rows = []
