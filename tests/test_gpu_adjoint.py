@@ -48,7 +48,15 @@ def test_energy_matches_oracle(oracle):
     assert e == pytest.approx(_oracle_energy(oracle, prog, an.a, an.b), abs=1e-12)
 
 
-def test_adjoint_all_gate_kinds_vs_oracle_fd(oracle):
+@pytest.fixture(params=["gates", "pauli"])
+def sweep(request, monkeypatch):
+    """Both single-wire sweep forms: per-gate passes, and one pass per wire with the gradients
+    formed from Pauli sums (the default from 22 qubits on)."""
+    monkeypatch.setenv("QGPU_ADJ_PAULI", "1" if request.param == "pauli" else "0")
+    return request.param
+
+
+def test_adjoint_all_gate_kinds_vs_oracle_fd(oracle, sweep):
     """Every invertible gate kind in the circuit (the sweep undoes each one)."""
     n = 6
     rng = np.random.default_rng(0)
@@ -72,7 +80,7 @@ def test_adjoint_all_gate_kinds_vs_oracle_fd(oracle):
     assert np.max(np.abs(g - fd)) <= 1e-7
 
 
-def test_adjoint_permutation_runs_vs_oracle_fd(oracle):
+def test_adjoint_permutation_runs_vs_oracle_fd(oracle, sweep):
     """Runs of CNot / X / Swap between rotation layers (undone as one index permutation each,
     out of place): gradients against the oracle's finite differences, and the register still
     holds the final state afterwards."""
@@ -102,6 +110,44 @@ def test_adjoint_permutation_runs_vs_oracle_fd(oracle):
     assert np.max(np.abs(g - fd)) <= 1e-7
     ref = oracle.simulate(prog, engine=oracle.DENSE)
     assert np.max(np.abs(h.download() - ref)) <= 1e-12
+
+
+def test_adjoint_long_single_wire_runs_vs_parameter_shift(sweep):
+    """Runs of up to seven single-wire gates on a wire (rotations of all kinds, Phase, and fixed
+    gates between them) undone together: every rotation's gradient against parameter shift."""
+    n = 9
+    rng = np.random.default_rng(21)
+    b = ProgramBuilder(n)
+    kinds = ["Rx", "Ry", "Rz", "Phase"]
+    for layer in range(2):
+        for w in range(n):
+            for q in range(1 + (w + layer) % 7):
+                if q % 3 == 2:
+                    b.add(["H", "S", "T", "X90", "MY90"][(w + q) % 5], w)
+                else:
+                    b.add(kinds[(w + q + layer) % 4], w, (), param=rng.uniform(-3, 3))
+        for w in range(0, n - 1, 2):
+            b.add("CNot", w + 1, (w,))
+        b.add("CZ", 0, (n - 1,))
+    prog = b.build()
+    a_c = rng.normal(size=n)
+    b_c = rng.normal(size=n)
+    h = nat.Handle(n)
+    e, g = GR.energy_and_gradient(h, prog, a_c, b_c)
+    ps = GR.parameter_shift(h, prog, a_c, b_c)
+    assert np.max(np.abs(g - ps)) <= 1e-9
+    assert math.isfinite(e)
+
+
+def test_adjoint_ansatz_22q_pauli_sweep_vs_parameter_shift():
+    """22 qubits (the vectors leave L2; the sweep takes the Pauli-sum form by default)."""
+    an = W.ansatz(n=22, layers=2, seed=7)
+    prog = an.program()
+    h = nat.Handle(22)
+    e, g = GR.energy_and_gradient(h, prog, an.a, an.b)
+    ps = GR.parameter_shift(h, prog, an.a, an.b)
+    assert np.max(np.abs(g - ps)) <= 1e-9
+    assert math.isfinite(e)
 
 
 def test_adjoint_ansatz_20q_vs_fd_and_parameter_shift():
