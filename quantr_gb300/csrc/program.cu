@@ -1220,10 +1220,12 @@ static int launch_pair(qgpu_handle* h, const PairBlock& pb, int lay) {
 }
 
 // ---- double pair passes: two 4x4 blocks on disjoint bit pairs of a 4-bit tile --------------
-// Each thread owns one tile of 16 amplitudes (full indices base | combinations of the 4 bits),
-// gathers them through the `pre` XOR terms, applies block A (the one on local bit 0) and block B,
-// and scatters them through the `post` terms. Every term flips only tile bits, so sources and
-// destinations are the thread's own 16 slots and the pass stays in place.
+// A tile is 16 amplitudes (full indices base | combinations of the 4 bits). Its amplitudes are
+// gathered through the slot permutation of the XOR terms folded before the blocks, block A (the
+// one on local bit 0) and block B are applied, and they are scattered through the permutation of
+// the terms folded after them. Every term flips only tile bits, so sources and destinations are
+// the tile's own 16 slots and the pass stays in place. complex128 (float pairs): four threads
+// share a tile (k_pair2); complex64: one thread holds it (k_pair2_f32).
 struct Pair2Params {
     uint64_t ngroups;                   // dim / 16
     int bits[4];                        // full-index bits, ascending
