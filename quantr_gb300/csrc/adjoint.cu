@@ -415,14 +415,18 @@ static bool affine_tables(const qgpu_op* ops, size_t n_ops, int n, std::vector<u
     return true;
 }
 
-// grads[g] = sum over blocks of partial[g * nb + b], for g in [0, ng)
+// out[g] = sum over blocks of partial[g * nb + b], for g in [0, ng): one warp per row (lanes
+// stride over the blocks, then a fixed shuffle tree; the order is the same on every run)
 __global__ void k_sum_partials(const double* __restrict__ partial, int nb, int ng,
                                double* __restrict__ out) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= ng) return;
+    const int g = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (g >= ng) return;  // whole warps leave together
     double s = 0.0;
-    for (int b = 0; b < nb; ++b) s += partial[(size_t)g * nb + b];
-    out[g] = s;
+    for (int b = lane; b < nb; b += 32) s += partial[(size_t)g * nb + b];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(0xffffffffu, s, d);
+    if (lane == 0) out[g] = s;
 }
 
 static int adj_blocks(const qgpu_handle* h, uint64_t work) {
@@ -842,8 +846,8 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
     if (st != QGPU_OK) return st;
     if (nrows > (int)nrow_cap) return fail(QGPU_ERR_UNSUPPORTED, "adjoint: partial-sum rows overflow");
     if (nrows) {
-        k_sum_partials<<<(unsigned)((nrows + 127) / 128), 128, 0, h->stream>>>(partial, nb, nrows,
-                                                                                gsum);
+        k_sum_partials<<<(unsigned)((nrows + 3) / 4), 128, 0, h->stream>>>(partial, nb, nrows,
+                                                                            gsum);
         QGPU_CHECK_LAUNCH("k_sum_partials");
         h->launches++;
     }
