@@ -106,6 +106,51 @@ def test_random_columns_plan(emulator, oracle, tmp_path, seed):
         assert np.max(np.abs(out - ref)) <= TOL
 
 
+@pytest.mark.parametrize("seed", [3, 4])
+def test_double_pair_grouping_random_xor_layers(emulator, oracle, tmp_path, seed):
+    """Random layers of wire-pair blocks separated by random commuting XOR runs (CNots with
+    controls inside and outside the pair tiles, Toffolis, X): whatever the matching folds, the
+    plan equals the oracle."""
+    n = 12
+    rng = np.random.default_rng(seed)
+    b = ProgramBuilder(n)
+    for layer in range(6):
+        perm = rng.permutation(n)
+        pairs = [(int(perm[2 * i]), int(perm[2 * i + 1])) for i in range(n // 2)]
+        for a, c in pairs:  # two dense layers and a CNot per pair: one 4x4 block each
+            for w in (a, c):
+                b.add("Ry", w, (), param=float(rng.uniform(0, 6.3)))
+                b.add("Rz", w, (), param=float(rng.uniform(0, 6.3)))
+            b.add("CNot", c, (a,))
+            for w in (a, c):
+                b.add("Rx", w, (), param=float(rng.uniform(0, 6.3)))
+        # a commuting XOR run (targets distinct, never controls): CNots joining neighbouring
+        # pairs (foldable when the matching puts the two pairs in one tile), then X, CNot and
+        # Toffoli on the remaining wires with controls anywhere
+        targets, controls = set(), set()
+        for i in range(0, len(pairs) - 1, 2):
+            c, t = pairs[i][1], pairs[i + 1][0]
+            b.add("CNot", t, (c,))
+            targets.add(t)
+            controls.add(c)
+        free = [w for w in range(n) if w not in targets and w not in controls]
+        for t in rng.permutation(free)[: 2]:
+            t = int(t)
+            targets.add(t)
+            pool = [w for w in range(n) if w not in targets]
+            k = int(rng.integers(0, 3))
+            ctrls = tuple(int(x) for x in rng.choice(pool, size=k, replace=False))
+            controls.update(ctrls)
+            b.add(["X", "CNot", "Toffoli"][k], t, ctrls)
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    for group in (0, 1):
+        out, counts = run_plan(emulator, prog, tmp_path, 1, group=group)
+        assert np.max(np.abs(out - ref)) <= TOL
+        if group:
+            assert counts["pair2"] > 0 and counts["folded"] > 0
+
+
 def test_every_gate_plan(emulator, oracle, tmp_path):
     """Each gate kind on each wire with controls above and below (no Custom)."""
     n = 6
