@@ -1402,6 +1402,18 @@ static void launch_pair2_pol(qgpu_handle* h, int part, uint64_t blocks, double2*
     else k_pair2<P, 2><<<(unsigned)blocks, PAIR2_THREADS, 0, h->stream>>>(s, q);
 }
 
+bool pair2_tc_supported(const qgpu_handle* h);  // pair_tc.cu
+int launch_pair2_tc(qgpu_handle* h, const Plan& plan, const Pass& ps, const uint64_t pre_off[16],
+                    const uint64_t post_off[16]);
+
+// Double pair passes on the tensor cores (k_pair2_tc, complex128 resident layout): tuning knob
+// QGPU_PAIR2_TC=1, read per call. Its kernel reports bounded-wait timeouts through the handle's
+// error word, so plans run with it are synchronised at the end.
+static bool pair2_tc_enabled() {
+    const char* e = std::getenv("QGPU_PAIR2_TC");
+    return e && e[0] == '1';
+}
+
 static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, int lay) {
     // block A holds local bit 0 (the lowest tile bit)
     const PairBlock* a = &plan.pairs[ps.pair];
@@ -1424,6 +1436,12 @@ static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, int la
         slot_offsets(ps.bits, ps.pre, q.pre_off);
         slot_offsets(ps.bits, ps.post, q.post_off);
     };
+    if (lay == LAY_RES && pair2_tc_enabled() && pair2_tc_supported(h)) {  // tensor cores
+        uint64_t pre_off[16], post_off[16];
+        slot_offsets(ps.bits, ps.pre, pre_off);
+        slot_offsets(ps.bits, ps.post, post_off);
+        return launch_pair2_tc(h, plan, ps, pre_off, post_off);
+    }
     // four threads per 16-amplitude tile
     uint64_t blocks = std::max<uint64_t>(
         1, std::min<uint64_t>(((h->dim >> 4) + PAIR2_THREADS / 4 - 1) / (PAIR2_THREADS / 4),
@@ -1566,8 +1584,10 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
                 prof_names.push_back("k_ff_layout");
             } else if (ps->pair2 >= 0) {
                 prof_names.push_back(h->precision == QGPU_C64 ? "k_pair2<f32>"
-                                     : resident               ? "k_pair2<ffr>"
-                                                              : "k_pair2<ff>");
+                                     : (play == LAY_RES && pair2_tc_enabled() && pair2_tc_supported(h))
+                                         ? "k_pair2_tc"
+                                     : resident ? "k_pair2<ffr>"
+                                                : "k_pair2<ff>");
             } else if (ps->pair >= 0) {
                 prof_names.push_back(h->precision == QGPU_C64 ? "k_pair<f32>"
                                      : resident               ? "k_pair<ffr>"
@@ -1747,7 +1767,7 @@ extern "C" int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_o
                         plan_options_for(h), &plan);
     if (st != QGPU_OK) return st;
     // queued without a final synchronisation unless the plan can report a bounded-wait timeout
-    return run_plan(h, plan, pipe_enabled() != 0);
+    return run_plan(h, plan, pipe_enabled() != 0 || pair2_tc_enabled());
 }
 
 // One CTA waits, with the pipelined kernels' bounded poll, on an mbarrier phase that nothing

@@ -158,6 +158,49 @@ def test_commuting_cx_runs(oracle, precision):
     assert np.max(np.abs(out - ref)) <= tol
 
 
+@pytest.mark.parametrize("n", [11, 13, 16])
+def test_double_pair_passes_on_tensor_cores(oracle, monkeypatch, n):
+    """k_pair2_tc (QGPU_PAIR2_TC=1): the double pair passes of the brickwork + QFT family on the
+    tensor cores through 8-bit fixed-point slices; complex128 within the fused-mode bar."""
+    monkeypatch.setenv("QGPU_PAIR2_TC", "1")
+    prog = W.brickwork_qft(n=n, layers=20, seed=7)
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    h = nat.Handle(n, nat.QGPU_C128, nat.QGPU_MODE_FAST)
+    h.set_profiling(True)
+    h.apply(prog.ops, prog.mats, prog.none)
+    out = h.download()
+    prof = h.profile(reset=True)
+    h.close()
+    assert "k_pair2_tc" in prof  # the tensor-core kernel ran
+    assert np.max(np.abs(out - ref)) <= TOL_FAST
+    assert abs(np.sum(np.abs(out) ** 2) - 1.0) <= 1e-12
+
+
+def test_double_pair_passes_on_tensor_cores_folded_terms(oracle, monkeypatch):
+    """k_pair2_tc with XOR terms folded before and after the blocks (permutations inside the
+    16 x 16 tile matrix), random register."""
+    monkeypatch.setenv("QGPU_PAIR2_TC", "1")
+    n = 13
+    rng = np.random.default_rng(77)
+    reg = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    reg /= np.linalg.norm(reg)
+    b = ProgramBuilder(n)
+    for layer in range(8):
+        for w in range(n):
+            b.add("Ry", w, (), param=float(rng.uniform(0, 6.3)))
+            b.add("Rz", w, (), param=float(rng.uniform(0, 6.3)))
+        for w in range(layer % 2, n - 1, 2):
+            b.add("CNot", w + 1, (w,))
+        for w in range(n):
+            b.add("Rx", w, (), param=float(rng.uniform(0, 6.3)))
+        for w in range(1 - layer % 2, n - 1, 2):
+            b.add("CNot", w + 1, (w,))
+    prog = b.build()
+    ref = oracle.simulate(prog, reg, engine=oracle.DENSE)
+    out = run_gpu(prog, "fast", reg=reg)
+    assert np.max(np.abs(out - ref)) <= TOL_FAST
+
+
 @pytest.mark.parametrize("precision", [nat.QGPU_C128, nat.QGPU_C64])
 @pytest.mark.parametrize("n", [8, 13])
 def test_double_pair_passes_folded_xor_terms(oracle, precision, n):
