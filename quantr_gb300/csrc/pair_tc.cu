@@ -249,6 +249,248 @@ __global__ void __launch_bounds__(PTC_THREADS, 2) k_pair2_tc(double2* __restrict
     if (warp == 0) tc::dealloc(tmem, PTC_TCOLS);
 }
 
+// ---- warp-specialised version (QGPU_PAIR2_TC=2) ---------------------------------------------
+// Status: correct (the same parity tests), slower on GB300: 15.4 ms per 30-qubit pass against
+// 13.2 (k_pair2_tc) and 11.4 (k_pair2). With one warp of each role per SM sub-partition every role
+// is latency-bound; the splitting (64-bit conversions and integer slicing) is the longest.
+// One CTA per SM with three roles and two of everything (A operand, tensor-memory accumulator),
+// so that block b+1 is split while block b is in the MMAs and block b-1 is recombined:
+//   warps 0-3  producers: one thread per tile row, all 16 amplitudes (the next block's loads are
+//              in flight while this one is split), writes A[s] and the row's scale exponent;
+//   warp 4     lane 0 issues the block's MMAs into accumulator s once A[s] is full and the
+//              consumers have released accumulator s, waits for them (bounded) and releases A[s]
+//              to the producers and the accumulator to the consumers;
+//   warps 5-8  consumers: one thread per tile row (tensor-memory lanes 32 (warp % 4) + lane),
+//              read the 7 weights, recombine, store, release the accumulator.
+// Hand-offs are mbarrier arrive (release) / bounded try_wait (acquire) pairs, counted per buffer
+// use: full[s] (128 producer arrivals), done[s] and empty[s] (the MMA thread), tfree[s] (128
+// consumer arrivals). Any wait that runs out sets the error word and stops that role; the others
+// then run out too, and the CTA frees its tensor memory after a final bounded wait.
+constexpr int PWS_THREADS = 288;
+constexpr uint32_t PWS_A_BYTES = PTC_A_BYTES;         // per buffer
+constexpr uint32_t PWS_TCOLS = 512;                   // two accumulators of 256 columns
+constexpr size_t PWS_SMEM = 2 * PWS_A_BYTES + PTC_B_BYTES + 4096;
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(PWS_THREADS, 1) k_pair2_ws(double2* __restrict__ st,
+                                                             const __grid_constant__ PairTcArgs a) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    uint8_t* sA0 = sm;
+    uint8_t* sB = sm + 2 * PWS_A_BYTES;
+    uint8_t* tail = sB + PTC_B_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(tail);  // full[2], empty[2], done[2], tfree[2], mma
+    uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 128);
+    int* abort_flag = reinterpret_cast<int*>(tail + 132);
+    // [4][128] scale exponents k of blocks it & 3: the producers of block it may only write once the
+    // consumers of block it - 4 have read (they released accumulator s before the MMAs of block
+    // it - 2, which released A[s] to the producers of block it)
+    int* sexp = reinterpret_cast<int*>(tail + 256);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t b_full = smem_u32(bars), b_empty = smem_u32(bars + 2), b_done = smem_u32(bars + 4),
+                   b_tfree = smem_u32(bars + 6), b_mma = smem_u32(bars + 8);
+
+    for (int i = tid; i < (int)(PTC_B_BYTES / 4); i += PWS_THREADS)
+        reinterpret_cast<uint32_t*>(sB)[i] = a.bimg[i];
+    const uint64_t o0 = 1ull << a.bits[0], o1 = 1ull << a.bits[1], o2 = 1ull << a.bits[2],
+                   o3 = 1ull << a.bits[3];
+    auto slot_off = [&](int j) {
+        return ((j & 1) ? o0 : 0) | ((j & 2) ? o1 : 0) | ((j & 4) ? o2 : 0) | ((j & 8) ? o3 : 0);
+    };
+    auto tile_base = [&](uint64_t blk, int r) {
+        return insert_zero(
+            insert_zero(insert_zero(insert_zero(blk * PTC_M + r, a.bits[0]), a.bits[1]), a.bits[2]),
+            a.bits[3]);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(b_full + 8 * s, PTC_M);
+            mbar_init(b_empty + 8 * s, 1);
+            mbar_init(b_done + 8 * s, 1);
+            mbar_init(b_tfree + 8 * s, PTC_M);
+        }
+        mbar_init(b_mma, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 4) tc::alloc(smem_u32(slot), PWS_TCOLS);
+    fence_proxy_async_shared();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint64_t nblocks = a.ntiles / PTC_M;
+    const uint64_t nmine = (nblocks > blockIdx.x) ? (nblocks - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    auto fail_now = [&]() {
+        atomicExch(a.err, 4);
+        atomicExch(abort_flag, 1);
+    };
+    auto aborted = [&]() { return *(volatile int*)abort_flag != 0; };
+
+    if (warp < 4) {  // ---------------------------------------------------------- producers
+        const int row = tid;
+        ffp nv[16];
+        if (nmine > 0) {
+            const uint64_t b0 = tile_base(blockIdx.x, row);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) nv[j] = ffr_load(st[b0 | slot_off(j)]);
+        }
+        for (uint64_t it = 0; it < nmine; ++it) {
+            const int s = (int)(it & 1);
+            ffp v[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = nv[j];
+            if (it + 1 < nmine) {  // the next block's loads fly while this one is split
+                const uint64_t bn = tile_base(blockIdx.x + (it + 1) * gridDim.x, row);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) nv[j] = ffr_load(st[bn | slot_off(j)]);
+            }
+            if (it >= 2 && !mbar_wait_bounded(b_empty + 8 * s, (uint32_t)(((it >> 1) - 1) & 1),
+                                              PTC_WAIT_LIMIT)) {
+                fail_now();
+                break;
+            }
+            if (aborted()) break;
+            int emax = 0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                float rh, ih;
+                up2(v[j].h, rh, ih);
+                emax = max(emax, (int)((__float_as_uint(rh) >> 23) & 0xFFu));
+                emax = max(emax, (int)((__float_as_uint(ih) >> 23) & 0xFFu));
+            }
+            const int k = 173 - emax;
+            const float f1 = pow2f(k / 2), f2 = pow2f(k - k / 2);
+            uint8_t* sA = sA0 + s * PWS_A_BYTES;
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {  // 4 slots (16 bytes of one slice) at a time
+                long long xr[4], xi[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float rh, ih, rl, il;
+                    up2(v[4 * c4 + q].h, rh, ih);
+                    up2(v[4 * c4 + q].l, rl, il);
+                    xr[q] = __float2ll_rn((rh * f1) * f2) + __float2ll_rn((rl * f1) * f2);
+                    xi[q] = __float2ll_rn((ih * f1) * f2) + __float2ll_rn((il * f1) * f2);
+                }
+#pragma unroll
+                for (int i = 0; i < 6; ++i) {
+                    uint32_t w4[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const float br = i < 5 ? byte_f((xr[q] >> (8 * i)) & 0xFF) : sbyte_f(xr[q] >> 40);
+                        const float bi = i < 5 ? byte_f((xi[q] >> (8 * i)) & 0xFF) : sbyte_f(xi[q] >> 40);
+                        w4[q] = bf16pair(br, bi);
+                    }
+                    *reinterpret_cast<uint4*>(sA + ptc_off(row, 32 * i + 8 * c4, PTC_SBO_A)) =
+                        make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                }
+            }
+            sexp[(int)(it & 3) * PTC_M + row] = k;
+            fence_proxy_async_shared();  // the generic-proxy writes of A become visible to the MMAs
+            mbar_arrive(b_full + 8 * s);
+        }
+    } else if (warp == 4) {  // ----------------------------------------------------- MMA issue
+        if (lane == 0) {
+            uint32_t mph = 0;
+            for (uint64_t it = 0; it < nmine; ++it) {
+                const int s = (int)(it & 1);
+                if (!mbar_wait_bounded(b_full + 8 * s, (uint32_t)((it >> 1) & 1), PTC_WAIT_LIMIT) ||
+                    (it >= 2 && !mbar_wait_bounded(b_tfree + 8 * s, (uint32_t)(((it >> 1) - 1) & 1),
+                                                   PTC_WAIT_LIMIT))) {
+                    fail_now();
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t sa = smem_u32(sA0 + s * PWS_A_BYTES), acc = tmem + 256u * (uint32_t)s;
+                auto mma = [&](int i, int jmin, int jend, int s0, bool init) {
+                    const uint32_t idesc = tc::idesc_bf16(PTC_M, 32 * (jend - jmin));
+#pragma unroll
+                    for (int kk = 0; kk < 2; ++kk) {
+                        const uint64_t ad = tc::smem_desc(sa + (uint32_t)(4 * i) * 128 + kk * 256, 128, PTC_SBO_A);
+                        const uint64_t bd = tc::smem_desc(
+                            smem_u32(sB) + (uint32_t)(4 * jmin) * PTC_SBO_B + kk * 256, 128, PTC_SBO_B);
+                        tc::mma_bf16(acc + (uint32_t)(32 * (s0 - 4)), ad, bd, idesc,
+                                     (init && kk == 0) ? 0u : 1u);
+                    }
+                };
+                mma(4, 0, 6, 4, true);
+                mma(5, 0, 5, 5, false);
+                mma(5, 5, 6, 10, true);
+                for (int i = 0; i < 4; ++i) mma(i, 4 - i, 6, 4, false);
+                tc::commit(b_mma);
+                const bool ok = mbar_wait_bounded(b_mma, mph, PTC_WAIT_LIMIT);
+                mph ^= 1u;
+                if (!ok) {
+                    fail_now();
+                    mbar_wait_bounded(b_mma, mph ^ 1u, PTC_WAIT_LIMIT);  // let it drain (bounded)
+                    break;
+                }
+                tc::fence_after_sync();
+                mbar_arrive(b_empty + 8 * s);  // A[s] may be rewritten
+                mbar_arrive(b_done + 8 * s);   // accumulator s holds block it
+            }
+        }
+    } else {  // ------------------------------------------------------------------- consumers
+        const int row = 32 * (warp & 3) + lane;
+        const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+        for (uint64_t it = 0; it < nmine; ++it) {
+            const int s = (int)(it & 1);
+            if (!mbar_wait_bounded(b_done + 8 * s, (uint32_t)((it >> 1) & 1), PTC_WAIT_LIMIT)) {
+                fail_now();
+                break;
+            }
+            tc::fence_after_sync();
+            const int k = sexp[(int)(it & 3) * PTC_M + row];
+            const uint64_t base = tile_base(blockIdx.x + it * gridDim.x, row);
+            const int c = -14 - k;
+            const u64 g1 = p2(pow2f(c / 2), pow2f(c / 2)), g2 = p2(pow2f(c - c / 2), pow2f(c - c / 2));
+#pragma unroll 1
+            for (int half = 0; half < 2; ++half) {
+                u64 ah[8], al[8];
+#pragma unroll
+                for (int w = 0; w < 7; ++w) {
+                    float d[16];
+                    tc::ld16(tmem + 256u * (uint32_t)s + lane_base + (uint32_t)(32 * w + 16 * half), d);
+                    const float sc = pow2f(8 * w);
+                    const u64 sc2 = p2(sc, sc);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const u64 t = pmul(p2(d[2 * u], d[2 * u + 1]), sc2);
+                        if (w == 0) {
+                            ah[u] = t;
+                            al[u] = 0;
+                        } else {
+                            const u64 s2 = padd(ah[u], t);
+                            const u64 bb = psub(s2, ah[u]);
+                            const u64 q = padd(psub(ah[u], psub(s2, bb)), psub(t, bb));
+                            ah[u] = s2;
+                            al[u] = padd(al[u], q);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const u64 hh = padd(ah[u], al[u]);
+                    const u64 ll = psub(al[u], psub(hh, ah[u]));
+                    ffp r;
+                    r.h = pmul(pmul(hh, g1), g2);
+                    r.l = pmul(pmul(ll, g1), g2);
+                    st[base | slot_off(8 * half + u)] = ffr_store(r);
+                }
+            }
+            tc::fence_before_sync();
+            mbar_arrive(b_tfree + 8 * s);  // accumulator s may be overwritten
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 4) tc::dealloc(tmem, PWS_TCOLS);
+}
+
 namespace {
 
 using cd = std::complex<double>;
@@ -310,20 +552,30 @@ static void build_pair_tc_image(const Plan& plan, const Pass& ps, const uint64_t
 }
 
 int launch_pair2_tc(qgpu_handle* h, const Plan& plan, const Pass& ps, const uint64_t pre_off[16],
-                    const uint64_t post_off[16]) {
+                    const uint64_t post_off[16], int variant) {
     static const cudaError_t attr =
         cudaFuncSetAttribute(k_pair2_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PTC_SMEM);
     QGPU_CUDA(attr);
+    static const cudaError_t attr_ws =
+        cudaFuncSetAttribute(k_pair2_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PWS_SMEM);
+    QGPU_CUDA(attr_ws);
     PairTcArgs a;
     std::memset(&a, 0, sizeof(a));
     a.ntiles = h->dim >> 4;
     for (int m = 0; m < 4; ++m) a.bits[m] = ps.bits[m];
     a.err = h->d_err;
     build_pair_tc_image(plan, ps, pre_off, post_off, a.bimg);
-    const uint64_t blocks =
-        std::max<uint64_t>(1, std::min<uint64_t>(a.ntiles / PTC_M, (uint64_t)h->sm_count * 2));
-    k_pair2_tc<<<(unsigned)blocks, PTC_THREADS, PTC_SMEM, h->stream>>>((double2*)cur_state(h), a);
-    QGPU_CHECK_LAUNCH("k_pair2_tc");
+    if (variant == 2) {  // warp-specialised: one CTA per SM
+        const uint64_t blocks =
+            std::max<uint64_t>(1, std::min<uint64_t>(a.ntiles / PTC_M, (uint64_t)h->sm_count));
+        k_pair2_ws<<<(unsigned)blocks, PWS_THREADS, PWS_SMEM, h->stream>>>((double2*)cur_state(h), a);
+        QGPU_CHECK_LAUNCH("k_pair2_ws");
+    } else {
+        const uint64_t blocks =
+            std::max<uint64_t>(1, std::min<uint64_t>(a.ntiles / PTC_M, (uint64_t)h->sm_count * 2));
+        k_pair2_tc<<<(unsigned)blocks, PTC_THREADS, PTC_SMEM, h->stream>>>((double2*)cur_state(h), a);
+        QGPU_CHECK_LAUNCH("k_pair2_tc");
+    }
     h->launches++;
     h->h2d_bytes += sizeof(a);
     return QGPU_OK;

@@ -1404,15 +1404,16 @@ static void launch_pair2_pol(qgpu_handle* h, int part, uint64_t blocks, double2*
 
 bool pair2_tc_supported(const qgpu_handle* h);  // pair_tc.cu
 int launch_pair2_tc(qgpu_handle* h, const Plan& plan, const Pass& ps, const uint64_t pre_off[16],
-                    const uint64_t post_off[16]);
+                    const uint64_t post_off[16], int variant);
 
 // Double pair passes on the tensor cores (k_pair2_tc, complex128 resident layout): tuning knob
 // QGPU_PAIR2_TC=1, read per call. Its kernel reports bounded-wait timeouts through the handle's
 // error word, so plans run with it are synchronised at the end.
-static bool pair2_tc_enabled() {
+static int pair2_tc_variant() {  // 0 off, 1 k_pair2_tc, 2 warp-specialised k_pair2_ws
     const char* e = std::getenv("QGPU_PAIR2_TC");
-    return e && e[0] == '1';
+    return (e && (e[0] == '1' || e[0] == '2')) ? e[0] - '0' : 0;
 }
+static bool pair2_tc_enabled() { return pair2_tc_variant() != 0; }
 
 static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, int lay) {
     // block A holds local bit 0 (the lowest tile bit)
@@ -1440,7 +1441,7 @@ static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, int la
         uint64_t pre_off[16], post_off[16];
         slot_offsets(ps.bits, ps.pre, pre_off);
         slot_offsets(ps.bits, ps.post, post_off);
-        return launch_pair2_tc(h, plan, ps, pre_off, post_off);
+        return launch_pair2_tc(h, plan, ps, pre_off, post_off, pair2_tc_variant());
     }
     // four threads per 16-amplitude tile
     uint64_t blocks = std::max<uint64_t>(
@@ -1585,7 +1586,7 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
             } else if (ps->pair2 >= 0) {
                 prof_names.push_back(h->precision == QGPU_C64 ? "k_pair2<f32>"
                                      : (play == LAY_RES && pair2_tc_enabled() && pair2_tc_supported(h))
-                                         ? "k_pair2_tc"
+                                         ? (pair2_tc_variant() == 2 ? "k_pair2_ws" : "k_pair2_tc")
                                      : resident ? "k_pair2<ffr>"
                                                 : "k_pair2<ff>");
             } else if (ps->pair >= 0) {

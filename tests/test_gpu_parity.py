@@ -158,11 +158,13 @@ def test_commuting_cx_runs(oracle, precision):
     assert np.max(np.abs(out - ref)) <= tol
 
 
+@pytest.mark.parametrize("variant", ["1", "2"])
 @pytest.mark.parametrize("n", [11, 13, 16])
-def test_double_pair_passes_on_tensor_cores(oracle, monkeypatch, n):
-    """k_pair2_tc (QGPU_PAIR2_TC=1): the double pair passes of the brickwork + QFT family on the
-    tensor cores through 8-bit fixed-point slices; complex128 within the fused-mode bar."""
-    monkeypatch.setenv("QGPU_PAIR2_TC", "1")
+def test_double_pair_passes_on_tensor_cores(oracle, monkeypatch, n, variant):
+    """k_pair2_tc (QGPU_PAIR2_TC=1) and its warp-specialised form k_pair2_ws (=2): the double
+    pair passes of the brickwork + QFT family on the tensor cores through 8-bit fixed-point
+    slices; complex128 within the fused-mode bar."""
+    monkeypatch.setenv("QGPU_PAIR2_TC", variant)
     prog = W.brickwork_qft(n=n, layers=20, seed=7)
     ref = oracle.simulate(prog, engine=oracle.DENSE)
     h = nat.Handle(n, nat.QGPU_C128, nat.QGPU_MODE_FAST)
@@ -171,15 +173,16 @@ def test_double_pair_passes_on_tensor_cores(oracle, monkeypatch, n):
     out = h.download()
     prof = h.profile(reset=True)
     h.close()
-    assert "k_pair2_tc" in prof  # the tensor-core kernel ran
+    assert ("k_pair2_ws" if variant == "2" else "k_pair2_tc") in prof  # the tensor-core kernel ran
     assert np.max(np.abs(out - ref)) <= TOL_FAST
     assert abs(np.sum(np.abs(out) ** 2) - 1.0) <= 1e-12
 
 
-def test_double_pair_passes_on_tensor_cores_folded_terms(oracle, monkeypatch):
-    """k_pair2_tc with XOR terms folded before and after the blocks (permutations inside the
-    16 x 16 tile matrix), random register."""
-    monkeypatch.setenv("QGPU_PAIR2_TC", "1")
+@pytest.mark.parametrize("variant", ["1", "2"])
+def test_double_pair_passes_on_tensor_cores_folded_terms(oracle, monkeypatch, variant):
+    """The tensor-core passes with XOR terms folded before and after the blocks (permutations
+    inside the 16 x 16 tile matrix), random register."""
+    monkeypatch.setenv("QGPU_PAIR2_TC", variant)
     n = 13
     rng = np.random.default_rng(77)
     reg = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
