@@ -80,9 +80,47 @@ __device__ __forceinline__ float pow2f(int e) {  // 2^e for -126 <= e <= 127
     return __int_as_float((e + 127) << 23);
 }
 
+// the float pair h + l scaled by f1 f2 (powers of two) and rounded to a 48-bit integer
+__device__ __forceinline__ long long fixed48(float h, float l, float f1, float f2) {
+    return __float2ll_rn((h * f1) * f2) + __float2ll_rn((l * f1) * f2);
+}
+// slice i (8 bits; slice 5 signed) of the real and imaginary parts, as one BF16 pair
+__device__ __forceinline__ uint32_t slice_pair(long long xr, long long xi, int i);
+
+// weight w of a recombination: (ah, al) += t 2^(8 w) in float pairs (TwoSum), both lanes
+__device__ __forceinline__ void add_weight(u64& ah, u64& al, float dr, float di, int w) {
+    const float sc = pow2f(8 * w);
+    const u64 t = pmul(p2(dr, di), p2(sc, sc));  // exact: a power of two
+    if (w == 0) {
+        ah = t;
+        al = 0;
+        return;
+    }
+    const u64 s = padd(ah, t);
+    const u64 bb = psub(s, ah);
+    const u64 q = padd(psub(ah, psub(s, bb)), psub(t, bb));
+    ah = s;
+    al = padd(al, q);
+}
+// the recombined pair normalised (FastTwoSum) and scaled by g1 g2 (powers of two)
+__device__ __forceinline__ ffp finish_pair(u64 ah, u64 al, u64 g1, u64 g2) {
+    const u64 hh = padd(ah, al);
+    const u64 ll = psub(al, psub(hh, ah));
+    ffp r;
+    r.h = pmul(pmul(hh, g1), g2);
+    r.l = pmul(pmul(ll, g1), g2);
+    return r;
+}
+
 __device__ __forceinline__ uint32_t bf16pair(float lo, float hi) {
     const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&p);
+}
+
+__device__ __forceinline__ uint32_t slice_pair(long long xr, long long xi, int i) {
+    const float br = i < 5 ? byte_f((xr >> (8 * i)) & 0xFF) : sbyte_f(xr >> 40);
+    const float bi = i < 5 ? byte_f((xi >> (8 * i)) & 0xFF) : sbyte_f(xi >> 40);
+    return bf16pair(br, bi);
 }
 
 __global__ void __launch_bounds__(PTC_THREADS, 2) k_pair2_tc(double2* __restrict__ st,
@@ -149,8 +187,8 @@ __global__ void __launch_bounds__(PTC_THREADS, 2) k_pair2_tc(double2* __restrict
             float rh, ih, rl, il;
             up2(v[u].h, rh, ih);
             up2(v[u].l, rl, il);
-            xr[u] = __float2ll_rn((rh * f1) * f2) + __float2ll_rn((rl * f1) * f2);
-            xi[u] = __float2ll_rn((ih * f1) * f2) + __float2ll_rn((il * f1) * f2);
+            xr[u] = fixed48(rh, rl, f1, f2);
+            xi[u] = fixed48(ih, il, f1, f2);
         }
         // slices into A: row = tile, k = 32 i + 2 slot + (re, im); 16 bytes = 4 slots of one slice
 #pragma unroll
@@ -159,12 +197,7 @@ __global__ void __launch_bounds__(PTC_THREADS, 2) k_pair2_tc(double2* __restrict
             for (int g = 0; g < 2; ++g) {
                 uint32_t w[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int u = 4 * g + q;
-                    const float br = i < 5 ? byte_f((xr[u] >> (8 * i)) & 0xFF) : sbyte_f(xr[u] >> 40);
-                    const float bi = i < 5 ? byte_f((xi[u] >> (8 * i)) & 0xFF) : sbyte_f(xi[u] >> 40);
-                    w[q] = bf16pair(br, bi);
-                }
+                for (int q = 0; q < 4; ++q) w[q] = slice_pair(xr[4 * g + q], xi[4 * g + q], i);
                 const int kk = 32 * i + 2 * (8 * half + 4 * g);
                 *reinterpret_cast<uint4*>(sA + ptc_off(row, kk, PTC_SBO_A)) =
                     make_uint4(w[0], w[1], w[2], w[3]);
@@ -210,34 +243,14 @@ __global__ void __launch_bounds__(PTC_THREADS, 2) k_pair2_tc(double2* __restrict
         for (int w = 0; w < 7; ++w) {
             float d[16];
             tc::ld16(tmem + lane_base + (uint32_t)(32 * w + 16 * half), d);
-            const float sc = pow2f(8 * w);
-            const u64 sc2 = p2(sc, sc);
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const u64 t = pmul(p2(d[2 * u], d[2 * u + 1]), sc2);  // exact: a power of two
-                if (w == 0) {
-                    ah[u] = t;
-                    al[u] = 0;
-                } else {
-                    const u64 s = padd(ah[u], t);  // TwoSum(ah, t)
-                    const u64 bb = psub(s, ah[u]);
-                    const u64 q = padd(psub(ah[u], psub(s, bb)), psub(t, bb));
-                    ah[u] = s;
-                    al[u] = padd(al[u], q);
-                }
-            }
+            for (int u = 0; u < 8; ++u) add_weight(ah[u], al[u], d[2 * u], d[2 * u + 1], w);
         }
         const int c = -14 - k;
         const u64 g1 = p2(pow2f(c / 2), pow2f(c / 2)), g2 = p2(pow2f(c - c / 2), pow2f(c - c / 2));
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const u64 hh = padd(ah[u], al[u]);  // FastTwoSum(ah, al)
-            const u64 ll = psub(al[u], psub(hh, ah[u]));
-            ffp r;
-            r.h = pmul(pmul(hh, g1), g2);
-            r.l = pmul(pmul(ll, g1), g2);
-            st[base | slot_off(8 * half + u)] = ffr_store(r);
-        }
+        for (int u = 0; u < 8; ++u)
+            st[base | slot_off(8 * half + u)] = ffr_store(finish_pair(ah[u], al[u], g1, g2));
         tc::fence_before_sync();
     }
     if (failed) {  // let an MMA still in flight finish (bounded) before freeing its accumulator
@@ -372,18 +385,14 @@ __global__ void __launch_bounds__(PWS_THREADS, 1) k_pair2_ws(double2* __restrict
                     float rh, ih, rl, il;
                     up2(v[4 * c4 + q].h, rh, ih);
                     up2(v[4 * c4 + q].l, rl, il);
-                    xr[q] = __float2ll_rn((rh * f1) * f2) + __float2ll_rn((rl * f1) * f2);
-                    xi[q] = __float2ll_rn((ih * f1) * f2) + __float2ll_rn((il * f1) * f2);
+                    xr[q] = fixed48(rh, rl, f1, f2);
+                    xi[q] = fixed48(ih, il, f1, f2);
                 }
 #pragma unroll
                 for (int i = 0; i < 6; ++i) {
                     uint32_t w4[4];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const float br = i < 5 ? byte_f((xr[q] >> (8 * i)) & 0xFF) : sbyte_f(xr[q] >> 40);
-                        const float bi = i < 5 ? byte_f((xi[q] >> (8 * i)) & 0xFF) : sbyte_f(xi[q] >> 40);
-                        w4[q] = bf16pair(br, bi);
-                    }
+                    for (int q = 0; q < 4; ++q) w4[q] = slice_pair(xr[q], xi[q], i);
                     *reinterpret_cast<uint4*>(sA + ptc_off(row, 32 * i + 8 * c4, PTC_SBO_A)) =
                         make_uint4(w4[0], w4[1], w4[2], w4[3]);
                 }
@@ -454,32 +463,12 @@ __global__ void __launch_bounds__(PWS_THREADS, 1) k_pair2_ws(double2* __restrict
                 for (int w = 0; w < 7; ++w) {
                     float d[16];
                     tc::ld16(tmem + 256u * (uint32_t)s + lane_base + (uint32_t)(32 * w + 16 * half), d);
-                    const float sc = pow2f(8 * w);
-                    const u64 sc2 = p2(sc, sc);
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const u64 t = pmul(p2(d[2 * u], d[2 * u + 1]), sc2);
-                        if (w == 0) {
-                            ah[u] = t;
-                            al[u] = 0;
-                        } else {
-                            const u64 s2 = padd(ah[u], t);
-                            const u64 bb = psub(s2, ah[u]);
-                            const u64 q = padd(psub(ah[u], psub(s2, bb)), psub(t, bb));
-                            ah[u] = s2;
-                            al[u] = padd(al[u], q);
-                        }
-                    }
+                    for (int u = 0; u < 8; ++u) add_weight(ah[u], al[u], d[2 * u], d[2 * u + 1], w);
                 }
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const u64 hh = padd(ah[u], al[u]);
-                    const u64 ll = psub(al[u], psub(hh, ah[u]));
-                    ffp r;
-                    r.h = pmul(pmul(hh, g1), g2);
-                    r.l = pmul(pmul(ll, g1), g2);
-                    st[base | slot_off(8 * half + u)] = ffr_store(r);
-                }
+                for (int u = 0; u < 8; ++u)
+                    st[base | slot_off(8 * half + u)] = ffr_store(finish_pair(ah[u], al[u], g1, g2));
             }
             tc::fence_before_sync();
             mbar_arrive(b_tfree + 8 * s);  // accumulator s may be overwritten
