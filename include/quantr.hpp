@@ -12,7 +12,10 @@
 #pragma once
 
 #include <algorithm>
+#include <charconv>
+#include <cmath>
 #include <complex>
+#include <cstdio>
 #include <cstdint>
 #include <functional>
 #include <iostream>
@@ -39,6 +42,74 @@ struct QuantrError : std::runtime_error {
 
 inline void check(int status) {
     if (status != QGPU_OK) throw QuantrError(qgpu_last_error());
+}
+
+inline uint64_t& shot_seed() {
+    static uint64_t s = 0;
+    return s;
+}
+// `fastrand::seed` counterpart: reseeds the stream that keys each measure_all call and the draws
+// of SuperPosition::measure.
+inline void seed(uint64_t s) { shot_seed() = s; }
+// one uniform double in [0, 1) from the shot stream: the stream steps (64-bit LCG) and its state
+// goes through the SplitMix64 finaliser; (x >> 11) 2^-53
+inline double next_shot_uniform() {
+    uint64_t z = shot_seed() = shot_seed() * 6364136223846793005ull + 1442695040888963407ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// an f64 as Rust's `{}` prints it: the fewest digits that read back to the same value, never an
+// exponent (2.0 -> "2", 1e-7 -> "0.0000001")
+inline std::string rust_f64(double x) {
+    if (std::isnan(x)) return "NaN";
+    if (std::isinf(x)) return x > 0 ? "inf" : "-inf";
+    char buf[400];
+    const auto r = std::to_chars(buf, buf + sizeof buf, x, std::chars_format::fixed);
+    return std::string(buf, r.ptr);
+}
+// an f64 as Rust's `{:?}` prints it: like `{}` with at least one fractional digit, but in
+// exponent form (no '+', no leading zeros: "1e-5", "1.5e16") below 1e-4 and from 1e16
+inline std::string rust_f64_debug(double x) {
+    if (std::isnan(x)) return "NaN";
+    if (std::isinf(x)) return x > 0 ? "inf" : "-inf";
+    const double a = std::fabs(x);
+    if (a == 0 || (a >= 1e-4 && a < 1e16)) {
+        std::string s = rust_f64(x);
+        if (s.find('.') == std::string::npos) s += ".0";
+        return s;
+    }
+    char buf[64];
+    const auto r = std::to_chars(buf, buf + sizeof buf, x, std::chars_format::scientific);
+    const std::string s(buf, r.ptr);  // shortest digits, e.g. "1e-05", "1.5e+16"
+    const size_t e = s.find('e');
+    return s.substr(0, e) + "e" + std::to_string(std::stoi(s.substr(e + 1)));
+}
+// a string as Rust's `{:?}` prints it: quoted, with \\, \", \n, \r, \t, \0 and other control
+// characters escaped
+inline std::string rust_str_debug(const std::string& v) {
+    std::string o = "\"";
+    for (unsigned char c : v) {
+        switch (c) {
+            case '\\': o += "\\\\"; break;
+            case '"': o += "\\\""; break;
+            case '\n': o += "\\n"; break;
+            case '\r': o += "\\r"; break;
+            case '\t': o += "\\t"; break;
+            case '\0': o += "\\0"; break;
+            default:
+                if (c < 0x20 || c == 0x7f) {
+                    char b[16];
+                    std::snprintf(b, sizeof b, "\\u{%x}", c);
+                    o += b;
+                } else {
+                    o += (char)c;
+                }
+        }
+    }
+    return o + "\"";
 }
 
 // ---- states (src/circuit/states/) -----------------------------------------------------------
@@ -78,11 +149,15 @@ class ProductState {
         qubits[place] = qubits[place] == Qubit::Zero ? Qubit::One : Qubit::Zero;
         return *this;
     }
-    ProductState kronecker_prod(Qubit q) const {
+    ProductState kronecker_prod(Qubit q) const {  // product_states.rs:180-183
         ProductState p = *this;
         p.qubits.push_back(q);
         return p;
     }
+    static ProductState from(Qubit q) { return ProductState({q}); }  // From<Qubit>
+    // the qubits in order (product_states_iter.rs)
+    std::vector<Qubit>::const_iterator begin() const { return qubits.begin(); }
+    std::vector<Qubit>::const_iterator end() const { return qubits.end(); }
     std::string to_string() const {
         std::string s;
         for (Qubit q : qubits) s += q == Qubit::One ? '1' : '0';
@@ -92,7 +167,26 @@ class ProductState {
     bool operator<(const ProductState& o) const { return qubits < o.qubits; }
 };
 
+// Qubit::kronecker_prod (qubit.rs:35-37): |a> (x) |b> = |ab>
+inline ProductState kronecker_prod(Qubit a, Qubit b) { return ProductState({a, b}); }
+
 class SuperPosition {
+    // |num - cmp| < 1e-6 (super_positions.rs:18, 246-248)
+    static bool equal_within_error(double num, double cmp) {
+        return num < cmp + 1e-6 && num > cmp - 1e-6;
+    }
+    static double norm_sqr_sum(const std::vector<Complex64>& a) {  // sequential, like `.sum()`
+        double t = 0;
+        for (const Complex64& x : a) t += x.real() * x.real() + x.imag() * x.imag();
+        return t;
+    }
+    static size_t trailing_zeros(size_t len) {  // usize::trailing_zeros (64 for 0)
+        size_t n = 0;
+        if (len == 0) return 8 * sizeof(size_t);
+        while (!((len >> n) & 1u)) ++n;
+        return n;
+    }
+
    public:
     std::vector<Complex64> amplitudes;
     size_t product_dim = 0;
@@ -105,29 +199,50 @@ class SuperPosition {
         a[0] = 1.0;
         return SuperPosition(std::move(a), n);
     }
-    static SuperPosition new_with_amplitudes(const std::vector<Complex64>& a) {
-        double t = 0;
-        for (auto& x : a) t += std::norm(x);
-        if (!(t > 1 - 1e-6 && t < 1 + 1e-6))
+    static SuperPosition new_with_amplitudes(const std::vector<Complex64>& a) {  // super_positions.rs:68-91
+        if (!equal_within_error(norm_sqr_sum(a), 1.0))
             throw QuantrError("Slice given to set amplitudes in super position does not conserve "
                               "probability, the absolute square sum of the coefficents must be one.");
         const size_t len = a.size();
         if (len == 0 || (len & (len - 1)))
             throw QuantrError("The length of the array must be of the form 2**n where n is an integer.");
-        size_t n = 0;
-        while (((size_t)1 << n) < len) ++n;
-        return SuperPosition(a, n);
+        return SuperPosition(a, trailing_zeros(len));
     }
+    // super_positions_unchecked.rs:64-70: no checks; the product dimension is the length's
+    // trailing zero count
     static SuperPosition new_with_amplitudes_unchecked(const std::vector<Complex64>& a) {
-        size_t n = 0;
-        while (((size_t)1 << n) < a.size()) ++n;
-        return SuperPosition(a, n);
+        return SuperPosition(a, trailing_zeros(a.size()));
+    }
+    // super_positions.rs:105-131: states missing from the map have amplitude zero
+    static SuperPosition new_with_hash_amplitudes(const std::map<ProductState, Complex64>& h) {
+        if (h.empty())
+            throw QuantrError("An empty HashMap was given. A superposition must have at least one "
+                              "non-zero state.");
+        const size_t dim = h.begin()->first.num_qubits();
+        double total = 0;
+        for (const auto& [st, amp] : h) {
+            if (st.num_qubits() != dim)
+                throw QuantrError("The first state has product dimension of " + std::to_string(dim) +
+                                  ", whilst the state, |" + st.to_string() +
+                                  ">, found as a key in the HashMap has dimension " +
+                                  std::to_string(st.num_qubits()) + ".");
+            total += amp.real() * amp.real() + amp.imag() * amp.imag();
+        }
+        if (!equal_within_error(total, 1.0))
+            throw QuantrError("The total sum of the absolute square of all amplitudes, " +
+                              rust_f64(total) +
+                              ", does not equal 1. That is, the superpositon does not conserve "
+                              "probability.");
+        std::vector<Complex64> a((size_t)1 << dim);
+        for (const auto& [st, amp] : h) a[st.comp_basis()] = amp;
+        return SuperPosition(std::move(a), dim);
     }
     static SuperPosition from(const ProductState& p) {
         std::vector<Complex64> a((size_t)1 << p.num_qubits());
         a[p.comp_basis()] = 1.0;
         return SuperPosition(std::move(a), p.num_qubits());
     }
+    static SuperPosition from(Qubit q) { return from(ProductState::from(q)); }
     std::optional<Complex64> get_amplitude(size_t i) const {
         if (i < amplitudes.size()) return amplitudes[i];
         return std::nullopt;
@@ -137,19 +252,90 @@ class SuperPosition {
     const std::vector<Complex64>& get_amplitudes() const { return amplitudes; }
     Complex64 get_amplitude_from_state(const ProductState& p) const {
         if (((size_t)1 << p.num_qubits()) != amplitudes.size())
-            throw QuantrError("Unable to retreive product state, |" + p.to_string() +
-                              "> with dimension " + std::to_string(p.num_qubits()) +
+            throw QuantrError("Unable to retreive product state, |\"" + p.to_string() +
+                              "\"> with dimension " + std::to_string(p.num_qubits()) +
                               ". The superposition is a linear combination of states with "
                               "different dimension. These dimensions should be equal.");
         return amplitudes[p.comp_basis()];
     }
+    SuperPosition& set_amplitudes(const std::vector<Complex64>& a) {  // super_positions.rs:229-244
+        if (a.size() != amplitudes.size())
+            throw QuantrError("The slice given to set the amplitudes in the computational basis has "
+                              "length " + std::to_string(a.size()) + ", when it should have length " +
+                              std::to_string(amplitudes.size()) + ".");
+        if (!equal_within_error(norm_sqr_sum(a), 1.0))
+            throw QuantrError("Slice given to set amplitudes in super position does not conserve "
+                              "probability, the absolute square sum of the coefficents must be one.");
+        amplitudes = a;
+        return *this;
+    }
+    // super_positions_unchecked.rs:74-77: no checks, the product dimension is left as it was
+    SuperPosition& set_amplitudes_unchecked(const std::vector<Complex64>& a) {
+        amplitudes = a;
+        return *this;
+    }
+    // super_positions.rs:270-299: every state of the register takes its amplitude from the map,
+    // or zero
+    SuperPosition& set_amplitudes_from_states(const std::map<ProductState, Complex64>& h) {
+        if (h.empty())
+            throw QuantrError("An empty HashMap was given. A superposition must have at least one "
+                              "non-zero state.");
+        const size_t dim = trailing_zeros(amplitudes.size());
+        double total = 0;
+        for (const auto& [st, amp] : h) {
+            if (st.num_qubits() != dim)
+                throw QuantrError("The first state has product dimension of " + std::to_string(dim) +
+                                  ", whilst the state, |" + st.to_string() +
+                                  ">, found as a key in the HashMap has dimension " +
+                                  std::to_string(st.num_qubits()) + ".");
+            total += amp.real() * amp.real() + amp.imag() * amp.imag();
+        }
+        if (!equal_within_error(total, 1.0))
+            throw QuantrError("The total sum of the absolute square of all amplitudes does not equal "
+                              "1. That is, the superpositon does not conserve probability.");
+        std::fill(amplitudes.begin(), amplitudes.end(), Complex64(0.0, 0.0));
+        for (const auto& [st, amp] : h) amplitudes[st.comp_basis()] = amp;
+        return *this;
+    }
     std::map<ProductState, Complex64> to_hash_map() const {  // super_positions.rs:315-323
         std::map<ProductState, Complex64> m;
-        for (size_t i = 0; i < amplitudes.size(); ++i)
-            if (!(std::norm(amplitudes[i]) < 1e-6 && std::norm(amplitudes[i]) > -1e-6))
-                m[ProductState::binary_basis(i, product_dim)] = amplitudes[i];
+        for (size_t i = 0; i < amplitudes.size(); ++i) {
+            const double p = amplitudes[i].real() * amplitudes[i].real() +
+                             amplitudes[i].imag() * amplitudes[i].imag();
+            if (!equal_within_error(p, 0.0)) m[ProductState::binary_basis(i, product_dim)] = amplitudes[i];
+        }
         return m;
     }
+    // One shot of the host-side container (super_positions.rs:332-342): the first state whose
+    // running sum of |a_i|^2 exceeds u, or nothing when u reaches the total (a register left
+    // unnormalised by a non-unitary Custom gate). `measure()` draws u from the shot stream
+    // (quantr draws it with `fastrand::f64()`); registers on the device are sampled by
+    // SimulatedCircuit::measure_all.
+    std::optional<ProductState> measure_with(double u) const {
+        double cum = 0;
+        for (size_t i = 0; i < amplitudes.size(); ++i) {
+            cum += amplitudes[i].real() * amplitudes[i].real() + amplitudes[i].imag() * amplitudes[i].imag();
+            if (u < cum) return ProductState::binary_basis(i, product_dim);
+        }
+        return std::nullopt;
+    }
+    std::optional<ProductState> measure() const { return measure_with(next_shot_uniform()); }
+    // `for (auto [state, amp] : superpos)` (super_position_iter.rs:19-47): every basis state in
+    // index order with its amplitude
+    struct Iter {
+        const SuperPosition* sp;
+        size_t i;
+        std::pair<ProductState, Complex64> operator*() const {
+            return {ProductState::binary_basis(i, sp->product_dim), sp->amplitudes[i]};
+        }
+        Iter& operator++() {
+            ++i;
+            return *this;
+        }
+        bool operator!=(const Iter& o) const { return i != o.i; }
+    };
+    Iter begin() const { return {this, 0}; }
+    Iter end() const { return {this, amplitudes.size()}; }
 };
 
 // ---- gates (src/circuit/gate.rs:19-106) --------------------------------------------------------
@@ -215,6 +401,39 @@ struct Gate {
                func_id == o.func_id && name == o.name;
     }
     bool operator!=(const Gate& o) const { return !(*this == o); }
+    // `{:?}` of the Rust enum (the `#[derive(Debug)]` of gate.rs:18), as quantr's validation
+    // messages print it: "H", "Rx(0.5)", "CRk(3, 1)", "Toffoli(0, 2)"; a Custom gate's function
+    // pointer prints as its address
+    std::string debug() const {
+        static const char* const names[] = {
+            "Id", "H", "X", "Y", "Z", "S", "Sdag", "T", "Tdag", "Rx", "Ry", "Rz", "X90", "Y90",
+            "MX90", "MY90", "Phase", "CR", "CRk", "CZ", "CY", "CNot", "Swap", "Toffoli", "Custom"};
+        const std::string nm = kind >= 0 && kind < QGPU_GATE_COUNT ? names[kind] : "?";
+        auto list = [](const std::vector<size_t>& v) {
+            std::string o = "[";
+            for (size_t i = 0; i < v.size(); ++i) o += (i ? ", " : "") + std::to_string(v[i]);
+            return o + "]";
+        };
+        switch (kind) {
+            case QGPU_GATE_RX: case QGPU_GATE_RY: case QGPU_GATE_RZ: case QGPU_GATE_PHASE:
+                return nm + "(" + rust_f64_debug(angle) + ")";
+            case QGPU_GATE_CR:
+                return nm + "(" + rust_f64_debug(angle) + ", " + std::to_string(controls[0]) + ")";
+            case QGPU_GATE_CRK:
+                return nm + "(" + std::to_string(k) + ", " + std::to_string(controls[0]) + ")";
+            case QGPU_GATE_CZ: case QGPU_GATE_CY: case QGPU_GATE_CNOT: case QGPU_GATE_SWAP:
+                return nm + "(" + std::to_string(controls[0]) + ")";
+            case QGPU_GATE_TOFFOLI:
+                return nm + "(" + std::to_string(controls[0]) + ", " + std::to_string(controls[1]) + ")";
+            case QGPU_GATE_CUSTOM: {
+                char a[32];
+                std::snprintf(a, sizeof a, "%p", func_id);
+                return nm + "(" + a + ", " + list(controls) + ", " + rust_str_debug(name) + ")";
+            }
+            default:
+                return nm;
+        }
+    }
 };
 
 template <class T>
@@ -229,13 +448,6 @@ struct HandleDeleter {
     void operator()(qgpu_handle* h) const { qgpu_destroy(h); }
 };
 using Handle = std::unique_ptr<qgpu_handle, HandleDeleter>;
-
-inline uint64_t& shot_seed() {
-    static uint64_t s = 0;
-    return s;
-}
-// `fastrand::seed` counterpart: reseeds the stream that keys each measure_all call.
-inline void seed(uint64_t s) { shot_seed() = s; }
 
 // The flat gate list as a gate program (simulation.rs:37-56): `Id` skipped, wire = index % n,
 // every Custom tabulated by calling its function on each local basis state
@@ -515,22 +727,30 @@ class Circuit {
         gates.insert(gates.end(), extended.begin(), extended.end());
     }
 
-    void overlapping(const std::vector<Gate>& gates) const {  // circuit.rs:272-293
+    // circuit.rs:272-293, in its order: repeated nodes, then a node on the gate's own wire. A
+    // node beyond the register is reported first with the crate's message for it (quantr's own
+    // repeat scan indexes past its table there and panics before reaching that message).
+    void overlapping(const std::vector<Gate>& gates) const {
         for (size_t pos = 0; pos < gates.size(); ++pos) {
             auto nodes = gates[pos].get_nodes();
             if (!nodes) continue;
-            std::vector<bool> seen(num_qubits_, false);
-            for (size_t nd : *nodes) {
+            for (size_t nd : *nodes)
                 if (nd >= num_qubits_)
                     throw QuantrError("The control node at position " + std::to_string(nd) +
                                       ", is greater than the umnber of qubits " +
                                       std::to_string(num_qubits_) + ".");
-                if (seen[nd]) throw QuantrError("The gate has overlapping control nodes.");
+            std::vector<bool> seen(num_qubits_, false);
+            for (size_t nd : *nodes) {
+                if (seen[nd])
+                    throw QuantrError("The gate, " + gates[pos].debug() +
+                                      ", has overlapping control nodes.");
                 seen[nd] = true;
-                if (nd == pos)
-                    throw QuantrError("The gate has a control node that equals the gate's position " +
-                                      std::to_string(pos) + ".");
             }
+            for (size_t nd : *nodes)
+                if (nd == pos)
+                    throw QuantrError("The gate, " + gates[pos].debug() +
+                                      ", has a control node that equals the gate's position " +
+                                      std::to_string(pos) + ".");
         }
     }
 

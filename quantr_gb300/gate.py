@@ -7,6 +7,8 @@ from __future__ import annotations
 
 from typing import Callable, Optional
 
+from .errors import rust_debug_f64, rust_debug_str
+
 
 class Gate:
     __slots__ = ("name", "args")
@@ -103,12 +105,17 @@ class Gate:
     def __hash__(self) -> int:
         return hash((self.name, self.args))
 
-    def __repr__(self) -> str:  # Rust Debug formatting
+    def __repr__(self) -> str:
+        """`{:?}` of the Rust enum (the `#[derive(Debug)]` of gate.rs:18), as quantr's validation
+        messages print it: "H", "Rx(0.5)", "CRk(3, 1)"; a Custom gate's function prints as an
+        address, like a Rust function pointer."""
         if not self.args:
             return self.name
         if self.name == "Custom":
-            return f"Custom({getattr(self.args[0], '__name__', 'fn')}, {list(self.args[1])}, {self.args[2]!r})"
-        return f"{self.name}({', '.join(repr(a) for a in self.args)})"
+            nodes = ", ".join(str(int(c)) for c in self.args[1])
+            return f"Custom({id(self.args[0]):#x}, [{nodes}], {rust_debug_str(self.args[2])})"
+        parts = [rust_debug_f64(a) if isinstance(a, float) else str(a) for a in self.args]
+        return f"{self.name}({', '.join(parts)})"
 
 
 for _n in ("Id", "H", "X", "Y", "Z", "S", "Sdag", "T", "Tdag", "X90", "Y90", "MX90", "MY90"):

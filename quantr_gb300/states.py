@@ -11,7 +11,7 @@ from typing import Iterator
 
 import numpy as np
 
-from .errors import QuantrError
+from .errors import QuantrError, rust_display_f64
 
 ZERO_MARGIN = 1e-6  # super_positions.rs:18
 
@@ -156,7 +156,8 @@ class SuperPosition:
                                   f"{st.num_qubits()}.")
             total += abs(amp) ** 2
         if not _equal_within_error(total, 1.0):
-            raise QuantrError(f"The total sum of the absolute square of all amplitudes, {total}, "
+            raise QuantrError(f"The total sum of the absolute square of all amplitudes, "
+                              f"{rust_display_f64(total)}, "
                               "does not equal 1. That is, the superpositon does not conserve "
                               "probability.")
         a = np.zeros(1 << dim, dtype=np.complex128)
@@ -188,7 +189,7 @@ class SuperPosition:
 
     def get_amplitude_from_state(self, prod_state: ProductState) -> complex:
         if (1 << prod_state.num_qubits()) != self.amplitudes.size:
-            raise QuantrError(f"Unable to retreive product state, |{prod_state}> with dimension "
+            raise QuantrError(f"Unable to retreive product state, |\"{prod_state}\"> with dimension "
                               f"{prod_state.num_qubits()}. The superposition is a linear "
                               "combination of states with different dimension. These dimensions "
                               "should be equal.")

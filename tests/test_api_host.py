@@ -147,3 +147,50 @@ def test_no_oracle_in_product_package():
     for p in (ROOT / "quantr_gb300").rglob("*"):
         if p.suffix in (".py", ".cu", ".cuh", ".cpp", ".h"):
             assert not pat.search(p.read_text()), p
+
+
+def _message(make) -> str:
+    with pytest.raises(QuantrError) as e:
+        make()
+    return e.value.message
+
+
+def test_validation_messages_print_gates_as_the_crate_does():  # circuit.rs:272-293
+    # repeated nodes are found before a node on the gate's own wire
+    assert _message(lambda: Circuit(3).add_gates([Gate.CNot(0), Gate.Id, Gate.Id])) == \
+        "The gate, CNot(0), has a control node that equals the gate's position 0."
+    assert _message(lambda: Circuit(3).add_gates([Gate.Toffoli(0, 0), Gate.Id, Gate.Id])) == \
+        "The gate, Toffoli(0, 0), has overlapping control nodes."
+    assert _message(lambda: Circuit(3).add_gates_with_positions(
+        {2: Gate.H, 0: Gate.CNot(2), 1: Gate.CNot(3)})) == \
+        "The control node at position 3, is greater than the umnber of qubits 3."
+
+
+def test_gate_debug_format():  # `{:?}` of gate.rs:18-45
+    assert repr(Gate.H) == "H"
+    assert repr(Gate.Rx(0.5)) == "Rx(0.5)"
+    assert repr(Gate.Phase(1.0)) == "Phase(1.0)"
+    assert repr(Gate.Rz(1e-5)) == "Rz(1e-5)"
+    assert repr(Gate.CR(2.0, 1)) == "CR(2.0, 1)"
+    assert repr(Gate.CRk(3, 1)) == "CRk(3, 1)"
+    assert repr(Gate.Toffoli(0, 2)) == "Toffoli(0, 2)"
+    r = repr(Gate.Custom(G.example_cnot, [0, 1], 'q"x'))
+    assert r.startswith("Custom(0x") and r.endswith(', [0, 1], "q\\"x")')
+
+
+def test_f64_in_messages_as_rust_prints_it():
+    from quantr_gb300.errors import rust_debug_f64, rust_debug_str, rust_display_f64
+
+    assert [rust_display_f64(x) for x in (2.0, 0.5, 1e-7, 0.1 + 0.2, -0.0, 1e21)] == \
+        ["2", "0.5", "0.0000001", "0.30000000000000004", "-0", "1000000000000000000000"]
+    assert [rust_debug_f64(x) for x in (1.0, 0.5, 1e-5, -2.5e-7, 1e16, 1234.5)] == \
+        ["1.0", "0.5", "1e-5", "-2.5e-7", "1e16", "1234.5"]
+    assert rust_debug_str('a"b\\c\n') == '"a\\"b\\\\c\\n"'
+    # super_positions.rs:122 prints the total with `{}`
+    st = {ProductState([Qubit.Zero, Qubit.One]): 2 ** -0.5,
+          ProductState([Qubit.One, Qubit.Zero]): -0.5j * 2 ** -0.5}
+    assert _message(lambda: SuperPosition.new_with_hash_amplitudes(st)).startswith(
+        "The total sum of the absolute square of all amplitudes, 0.625")
+    s = SuperPosition.new(2)
+    assert _message(lambda: s.get_amplitude_from_state(ProductState([0, 1, 1]))).startswith(
+        'Unable to retreive product state, |"011"> with dimension 3.')
