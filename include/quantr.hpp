@@ -706,7 +706,9 @@ class Circuit {
                 for (unsigned char ch : g.name)
                     if (ch > 127)
                         throw QuantrError("The custom function name, " + g.name +
-                                          ", does not only use ASCII chars.");
+                                          ", does not only use ASCII chars. This could lead to "
+                                          "problems in printing the circuit diagram. This warning "
+                                          "will be promoted to an Error in the next major release.");
             if (g != Gate::Id()) {
                 if (found_multi) {
                     found_second = true;

@@ -183,6 +183,16 @@ int main() {
     CHECK(error_of([] { Circuit::new_(3).add_gates_with_positions({{2, Gate::H()}, {0, Gate::CNot(2)}, {1, Gate::CNot(3)}}); }) ==
           "The control node at position 3, is greater than the umnber of qubits 3.");
     CHECK(error_of([] { Circuit::new_(3).add_gates({Gate::CNot(1), Gate::Id(), Gate::Id()}); }).empty());
+    auto fn = [](const ProductState&) -> std::optional<SuperPosition> { return std::nullopt; };
+    CHECK(error_of([&] { Circuit::new_(3).add_gate(Gate::Custom(fn, {0}, "NonAscii\xe2\x80\xa0"), 1); }) ==
+          "The custom function name, NonAscii\xe2\x80\xa0, does not only use ASCII chars. This could "
+          "lead to problems in printing the circuit diagram. This warning will be promoted to an "
+          "Error in the next major release.");
+    CHECK(error_of([] { Circuit::new_(2).add_gates({Gate::H()}); }) ==
+          "The number of gates, 1, does not match the number of wires, 2. All wires must have gates added.");
+    CHECK(error_of([] { Circuit::new_(2).add_gate(Gate::H(), 2); }) ==
+          "The position, 2, is out of bounds for the circuit with 2 qubits.");
+    CHECK(error_of([] { Circuit::new_(0); }) == "The initialised circuit must have at least one wire.");
 
     std::printf("%d failure(s)\n", failures);
     return failures != 0;
