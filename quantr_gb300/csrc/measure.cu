@@ -25,7 +25,6 @@
 namespace qgpu {
 
 constexpr int CHUNK_BITS = 9;   // 512 amplitudes per chunk: 32 lanes x 16
-constexpr int PER_LANE = 16;
 constexpr int SCAN_TILE = 1024;
 
 template <class S>
