@@ -37,7 +37,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 from pathlib import Path
 
@@ -326,7 +325,7 @@ def run_reference(args) -> None:
 def run_ours(args) -> None:
     import torch
 
-    from quantr_gb300 import Circuit, _native as nat
+    from quantr_gb300 import _native as nat
     from quantr_gb300 import workloads as W
 
     world, rank, local = dist_setup()

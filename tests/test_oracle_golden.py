@@ -11,7 +11,7 @@ import pytest
 
 from golden import quantr_goldens as G
 from quantr_gb300 import Circuit, Gate, ProductState, Qubit, SuperPosition
-from quantr_gb300.program import ProgramBuilder, lower, tabulate_custom
+from quantr_gb300.program import ProgramBuilder, lower
 from quantr_gb300 import workloads as W
 
 
