@@ -1,7 +1,8 @@
 // Host-side executor of the fused pass plan (quantr_gb300/csrc/plan.cpp) in complex128, so the
 // planner's merging, pair fusion, table folding, XOR runs and pass grouping can be checked
 // against the oracle on a machine without a GPU. Steps are applied with their f64 entries
-// (DevStep::d) in the order and on the amplitudes the tile kernels use.
+// (DevStep::d) in the order and on the amplitudes the tile kernels use; Custom passes apply
+// their tabulated block with the None rule.
 //
 // usage: plan_emulator n ops.bin mats.bin none.bin out.bin [pair_fusion budget max_arith_bits
 //                                                          plan_only]
@@ -184,7 +185,7 @@ int main(int argc, char** argv) {
     const uint64_t dim = 1ull << n;
     std::vector<cd> st(dim);
     st[0] = 1.0;
-    int npair = 0, ntile = 0, nxor = 0, npair2 = 0;
+    int npair = 0, ntile = 0, nxor = 0, npair2 = 0, ncustom = 0;
     size_t nfolded = 0;
     // a 4x4 block on bits (hi, lo), local index 2 * bit(hi) + bit(lo)
     auto apply_block = [&](const qgpu::PairBlock& pb) {
@@ -234,8 +235,37 @@ int main(int argc, char** argv) {
             continue;
         }
         if (p.custom >= 0) {
-            std::fprintf(stderr, "custom passes are not emulated\n");
-            return 4;
+            // quantr's apply_gate with the None rule (simulation.rs:64-135): an output whose
+            // local input had no image keeps its amplitude; the others take the products of the
+            // inputs that have one (M column-major: M[j * 2^k + l] = image of input j at l)
+            ++ncustom;
+            const qgpu::LocalGate& g = plan.customs[p.custom];
+            const size_t kd = (size_t)1 << g.k;
+            std::vector<uint64_t> scatter(kd);
+            uint64_t acting = 0;
+            for (size_t l = 0; l < kd; ++l) {
+                uint64_t off = 0;
+                for (int m = 0; m < g.k; ++m)
+                    if ((l >> (g.k - 1 - m)) & 1u) off |= 1ull << (n - 1 - g.wires[m]);
+                scatter[l] = off;
+                acting |= off;
+            }
+            std::vector<cd> x(kd), y(kd);
+            for (uint64_t b = 0; b < dim; ++b) {
+                if (b & acting) continue;
+                for (size_t l = 0; l < kd; ++l) x[l] = st[b | scatter[l]];
+                for (size_t l = 0; l < kd; ++l) {
+                    if (g.none[l]) {
+                        y[l] = x[l];
+                        continue;
+                    }
+                    y[l] = 0.0;
+                    for (size_t j = 0; j < kd; ++j)
+                        if (!g.none[j]) y[l] += g.M[j * kd + l] * x[j];
+                }
+                for (size_t l = 0; l < kd; ++l) st[b | scatter[l]] = y[l];
+            }
+            continue;
         }
         if (p.pair >= 0) {
             ++npair;
@@ -294,7 +324,7 @@ int main(int argc, char** argv) {
     }
     std::ofstream out(argv[5], std::ios::binary);
     out.write(reinterpret_cast<const char*>(st.data()), (std::streamsize)(dim * sizeof(cd)));
-    std::printf("passes %zu pair %d tile %d xor %d pair2 %d folded %zu\n", plan.passes.size(), npair,
-                ntile, nxor, npair2, nfolded);
+    std::printf("passes %zu pair %d tile %d xor %d pair2 %d folded %zu custom %d\n",
+                plan.passes.size(), npair, ntile, nxor, npair2, nfolded, ncustom);
     return 0;
 }

@@ -210,3 +210,52 @@ def test_pair_blocks_interleaved_wires(emulator, oracle, tmp_path):
         out, counts = run_plan(emulator, prog, tmp_path, 1, group=group)
         assert counts["pair"] + counts["pair2"] > 0
         assert np.max(np.abs(out - ref)) <= TOL
+
+
+@pytest.mark.parametrize("seed", [5, 6])
+def test_custom_blocks_between_fused_passes(emulator, oracle, tmp_path, seed):
+    """Custom gates (dense blocks with None entries, a non-unitary one-wire block, a permutation
+    on six wires with controls above and below the target) inside runs of pair-fusable gates,
+    phase rows and CNot layers: the planner must close every open block and table at a Custom
+    gate and keep the gate order around it. (The None rule is folded into the tabulated matrix;
+    blocks left in controlled-2x2 form join the ordinary passes.)"""
+    n = 9
+    rng = np.random.default_rng(seed)
+    b = ProgramBuilder(n)
+    customs = 0
+    for layer in range(4):
+        for w in range(n):
+            b.add("Ry", w, (), param=float(rng.uniform(0, 6.3)))
+            b.add("Rz", w, (), param=float(rng.uniform(0, 6.3)))
+        for w in range(layer % 2, n - 1, 2):
+            b.add("CNot", w + 1, (w,))
+        t, c1, c2 = (int(x) for x in rng.choice(n, size=3, replace=False))
+        blk = rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8))
+        none = (rng.random(8) < 0.25).astype(np.uint8)
+        b.add_custom(t, [c1, c2], blk / 3, none)
+        customs += 1
+        for w in range(n):
+            b.add("Rx", w, (), param=float(rng.uniform(0, 6.3)))
+        b.add("H", 0)
+        for k in range(2, n + 1):
+            b.add("CRk", 0, (k - 1,), k=k)
+        w = int(rng.integers(0, n))
+        b.add_custom(w, [], np.array([[1.2, 0.1j], [0, 0.8]], np.complex128),
+                     np.array([0, layer % 2], np.uint8))
+        customs += 1
+    d = 1 << 6
+    wires = [int(x) for x in rng.choice(n, size=6, replace=False)]
+    perm = np.eye(d, dtype=np.complex128)[rng.permutation(d)] * np.exp(1j * rng.random(d))[:, None]
+    b.add_custom(wires[2], wires[:2] + wires[3:], perm, np.zeros(d, np.uint8))
+    customs += 1
+    for w in range(n):
+        b.add("Ry", w, (), param=float(rng.uniform(0, 6.3)))
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    scale = max(1.0, float(np.max(np.abs(ref))))
+    for pair in (0, 1):
+        for group in (0, 1):
+            out, counts = run_plan(emulator, prog, tmp_path, pair, group=group)
+            # blocks in controlled-2x2 form (every one-wire block) run as ordinary gates
+            assert 5 <= counts["custom"] <= customs
+            assert np.max(np.abs(out - ref)) <= TOL * scale
