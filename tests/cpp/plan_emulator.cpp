@@ -5,7 +5,8 @@
 // their tabulated block with the None rule.
 //
 // usage: plan_emulator n ops.bin mats.bin none.bin out.bin [pair_fusion budget max_arith_bits
-//                                                          plan_only]
+//                                                          plan_only group block_qubits max_gates]
+//   block_qubits > 0: dense-block fusion (build_blocks) instead of the pass plan
 //   ops.bin: qgpu_op records; mats.bin: f64; none.bin: u8; out.bin receives 2^n complex128.
 #include <algorithm>
 #include <cmath>
@@ -125,7 +126,8 @@ static void apply_step(const qgpu::DevStep& s, const qgpu::Pass& p, const qgpu::
 
 int main(int argc, char** argv) {
     if (argc < 6) {
-        std::fprintf(stderr, "usage: %s n ops mats none out [pair budget arith_bits plan_only group]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s n ops mats none out [pair budget arith_bits plan_only group "
+                             "block_qubits max_gates]\n", argv[0]);
         return 2;
     }
     const int n = std::atoi(argv[1]);
@@ -138,6 +140,46 @@ int main(int argc, char** argv) {
     opt.budget = argc > 7 ? std::atoi(argv[7]) : 280;
     opt.max_arith_bits = argc > 8 ? std::atoi(argv[8]) : 2;
     opt.group_pairs = argc > 10 ? std::atoi(argv[10]) != 0 : true;
+    if (argc > 12 && std::atoi(argv[11]) > 0) {
+        // dense-block fusion (build_blocks): each block's row-major matrix applied to the
+        // amplitudes of its bits (local bit m <-> full-index bit bits[m])
+        std::vector<qgpu::DenseBlock> blocks;
+        if (qgpu::build_blocks(ops.data(), ops.size(), n, mats.data(), mats.size(), none.data(),
+                               none.size(), std::atoi(argv[11]), std::atoi(argv[12]), &blocks) != QGPU_OK)
+            return 1;
+        const uint64_t dim = 1ull << n;
+        std::vector<cd> st(dim);
+        st[0] = 1.0;
+        int maxk = 0, gates = 0;
+        for (const qgpu::DenseBlock& b : blocks) {
+            maxk = std::max(maxk, b.k);
+            gates += b.gates;
+            const size_t D = (size_t)1 << b.k;
+            std::vector<uint64_t> off(D);
+            uint64_t mask = 0;
+            for (size_t c = 0; c < D; ++c) {
+                uint64_t o = 0;
+                for (int m = 0; m < b.k; ++m)
+                    if ((c >> m) & 1u) o |= 1ull << b.bits[m];
+                off[c] = o;
+                mask |= o;
+            }
+            std::vector<cd> x(D);
+            for (uint64_t base = 0; base < dim; ++base) {
+                if (base & mask) continue;
+                for (size_t c = 0; c < D; ++c) x[c] = st[base | off[c]];
+                for (size_t l = 0; l < D; ++l) {
+                    cd y = 0.0;
+                    for (size_t c = 0; c < D; ++c) y += b.M[l * D + c] * x[c];
+                    st[base | off[l]] = y;
+                }
+            }
+        }
+        std::ofstream out(argv[5], std::ios::binary);
+        out.write(reinterpret_cast<const char*>(st.data()), (std::streamsize)(dim * sizeof(cd)));
+        std::printf("blocks %zu maxk %d gates %d\n", blocks.size(), maxk, gates);
+        return 0;
+    }
     qgpu::Plan plan;
     if (qgpu::build_plan(ops.data(), ops.size(), n, mats.data(), mats.size(), none.data(),
                          none.size(), opt, &plan) != QGPU_OK)

@@ -259,3 +259,60 @@ def test_custom_blocks_between_fused_passes(emulator, oracle, tmp_path, seed):
             # blocks in controlled-2x2 form (every one-wire block) run as ordinary gates
             assert 5 <= counts["custom"] <= customs
             assert np.max(np.abs(out - ref)) <= TOL * scale
+
+
+def run_blocks(emulator, prog, tmp_path, block_qubits, max_gates):
+    f = {k: tmp_path / f"{k}.bin" for k in ("ops", "mats", "none", "out")}
+    np.ascontiguousarray(prog.ops).tofile(f["ops"])
+    np.ascontiguousarray(prog.mats, dtype=np.float64).tofile(f["mats"])
+    np.ascontiguousarray(prog.none, dtype=np.uint8).tofile(f["none"])
+    r = subprocess.run([str(emulator), str(prog.n), str(f["ops"]), str(f["mats"]), str(f["none"]),
+                        str(f["out"]), "1", "280", "2", "0", "1", str(block_qubits), str(max_gates)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    counts = dict(zip(r.stdout.split()[::2], map(int, r.stdout.split()[1::2])))
+    return np.fromfile(f["out"], dtype=np.complex128), counts
+
+
+@pytest.mark.parametrize("bq,mg", [(6, 12), (4, 5), (3, 4), (1, 1)])
+def test_dense_block_fusion(emulator, oracle, tmp_path, bq, mg):
+    """Dense-block fusion (build_blocks, the precision configuration's 6-qubit blocks of <= 12
+    gates): consecutive gates multiplied on the host into one matrix per block, Custom blocks
+    with None entries and a gate wider than the block limit (a block of its own) included. The
+    blocks applied in complex128 equal the oracle; no block exceeds the limit unless one gate
+    does; every non-identity gate lands in exactly one block."""
+    n = 9
+    rng = np.random.default_rng(17)
+    b = ProgramBuilder(n)
+    gates = 0
+    for w in range(n):
+        b.add("H", w)
+        gates += 1
+    for layer in range(3):
+        for w in range(n):
+            b.add("Ry", w, (), param=float(rng.uniform(0, 6.3)))
+            gates += 1
+        for w in range(layer % 2, n - 1, 2):
+            b.add("CNot", w + 1, (w,))
+            gates += 1
+        b.add("Toffoli", 4, (8, 0))
+        b.add_custom(2, [6], rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)),
+                     np.array([0, 1, 0, 0], np.uint8))
+        b.add("CRk", 1, (7,), k=4)
+        b.add("Swap", 3, (5,))
+        b.add("CR", 8, (2,), param=0.3)
+        gates += 5
+    d = 1 << 7
+    perm = np.eye(d, dtype=np.complex128)[rng.permutation(d)]
+    b.add_custom(5, [0, 1, 2, 3, 7, 8], perm, np.zeros(d, np.uint8))  # 7 wires
+    gates += 1
+    for w in range(n):
+        b.add("Rx", w, (), param=0.2 * w + 0.1)
+        gates += 1
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    out, counts = run_blocks(emulator, prog, tmp_path, bq, mg)
+    assert np.max(np.abs(out - ref)) <= TOL * max(1.0, float(np.max(np.abs(ref))))
+    assert counts["gates"] == gates
+    assert counts["maxk"] <= max(bq, 7)
+    assert counts["blocks"] >= -(-gates // mg)
