@@ -436,37 +436,6 @@ static int adj_blocks(const qgpu_handle* h, uint64_t work) {
     return (int)std::max<uint64_t>(1, b);
 }
 
-static bool is_rotation(int kind) {
-    return kind == QGPU_GATE_RX || kind == QGPU_GATE_RY || kind == QGPU_GATE_RZ ||
-           kind == QGPU_GATE_PHASE;
-}
-
-// The inverse of a non-Custom op as another op (U^dagger), quantr's conventions.
-static qgpu_op inverse_op(const qgpu_op& op) {
-    qgpu_op r = op;
-    switch (op.kind) {
-        case QGPU_GATE_S: r.kind = QGPU_GATE_SDAG; break;
-        case QGPU_GATE_SDAG: r.kind = QGPU_GATE_S; break;
-        case QGPU_GATE_T: r.kind = QGPU_GATE_TDAG; break;
-        case QGPU_GATE_TDAG: r.kind = QGPU_GATE_T; break;
-        case QGPU_GATE_X90: r.kind = QGPU_GATE_MX90; break;
-        case QGPU_GATE_MX90: r.kind = QGPU_GATE_X90; break;
-        case QGPU_GATE_Y90: r.kind = QGPU_GATE_MY90; break;
-        case QGPU_GATE_MY90: r.kind = QGPU_GATE_Y90; break;
-        case QGPU_GATE_RX: case QGPU_GATE_RY: case QGPU_GATE_RZ: case QGPU_GATE_PHASE:
-        case QGPU_GATE_CR:
-            r.param = -op.param;
-            break;
-        case QGPU_GATE_CRK:
-            r.kind = QGPU_GATE_CR;
-            r.param = -((2.0 * 3.14159265358979323846) / std::pow(2.0, (double)op.k));
-            break;
-        default:
-            break;  // H, X, Y, Z, CNot, CY, CZ, Swap, Toffoli are self-inverse
-    }
-    return r;
-}
-
 // Energy of the vector at `psi` into *energy; lambda = H psi left at `lam`.
 static int energy_into(qgpu_handle* h, const double2* psi, double2* lam, const Ham& H,
                        double* partial, double* energy) {
@@ -648,53 +617,12 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
             // and V P V^dag = q0 I + qx X + qy Y + qz Z: its gradient is that combination of the
             // Pauli sums, formed on the host.
             for (size_t w = 0; w < wires.size(); ++w) {
-                const std::vector<size_t>& gw = gates[w];  // reverse order: gw[0] is the last
-                const size_t k = gw.size();
-                std::vector<std::array<cd, 4>> fwd(k), inv(k);  // row-major 2x2: m[2 l + j]
-                for (size_t q = 0; q < k; ++q) {
-                    LocalGate a, b;
-                    int s3 = tabulate(ops[gw[q]], h->n_qubits, nullptr, 0, nullptr, 0, &a);
-                    if (s3 == QGPU_OK)
-                        s3 = tabulate(inverse_op(ops[gw[q]]), h->n_qubits, nullptr, 0, nullptr, 0, &b);
-                    if (s3 != QGPU_OK) return s3;
-                    for (int l = 0; l < 2; ++l)
-                        for (int j = 0; j < 2; ++j) {
-                            fwd[q][2 * l + j] = a.M[j * 2 + l];
-                            inv[q][2 * l + j] = b.M[j * 2 + l];
-                        }
-                }
-                auto mul = [](const std::array<cd, 4>& x, const std::array<cd, 4>& y) {
-                    return std::array<cd, 4>{x[0] * y[0] + x[1] * y[2], x[0] * y[1] + x[1] * y[3],
-                                             x[2] * y[0] + x[3] * y[2], x[2] * y[1] + x[3] * y[3]};
-                };
-                // undo = G_1^dag ... G_k^dag (G_k^dag applied first); V runs over the later gates
-                std::array<cd, 4> undo{cd(1), cd(0), cd(0), cd(1)}, V{cd(1), cd(0), cd(0), cd(1)};
-                bool need[5] = {false, false, false, false, false};
-                std::vector<std::pair<size_t, std::array<double, 5>>> rots;
-                for (size_t q = 0; q < k; ++q) {  // q = 0 is the last gate of the run
-                    undo = mul(inv[q], undo);
-                    const qgpu_op& op = ops[gw[q]];
-                    if (is_rotation(op.kind)) {
-                        std::array<cd, 4> P{cd(0), cd(0), cd(0), cd(0)};
-                        switch (op.kind) {
-                            case QGPU_GATE_RX: P = {cd(0), cd(1), cd(1), cd(0)}; break;
-                            case QGPU_GATE_RY: P = {cd(0), cd(0, -1), cd(0, 1), cd(0)}; break;
-                            case QGPU_GATE_RZ: P = {cd(1), cd(0), cd(0), cd(-1)}; break;
-                            default: P = {cd(-1), cd(0), cd(0), cd(-1)}; break;  // Phase: -I
-                        }
-                        const std::array<cd, 4> Vd{std::conj(V[0]), std::conj(V[2]), std::conj(V[1]),
-                                                   std::conj(V[3])};
-                        const std::array<cd, 4> Q = mul(mul(V, P), Vd);
-                        std::array<double, 5> c{};  // kinds 1 X, 2 Y, 3 Z, 4 -I
-                        c[1] = Q[2].real();
-                        c[2] = Q[2].imag();
-                        c[3] = 0.5 * (Q[0].real() - Q[3].real());
-                        c[4] = -0.5 * (Q[0].real() + Q[3].real());
-                        for (int m = 1; m <= 4; ++m) need[m] = need[m] || c[m] != 0.0;
-                        rots.emplace_back(gw[q], c);
-                    }
-                    V = mul(V, fwd[q]);  // the gates after the next one back
-                }
+                PauliRun pr;
+                int s3 = pauli_run(ops, gates[w], h->n_qubits, &pr);
+                if (s3 != QGPU_OK) return s3;
+                const std::array<cd, 4>& undo = pr.undo;
+                const bool* need = pr.need;
+                const auto& rots = pr.rots;
                 AdjTileParams p;
                 std::memset(&p, 0, sizeof(p));
                 p.nbits = 1;

@@ -1349,4 +1349,87 @@ int build_blocks(const qgpu_op* ops, size_t n_ops, int n, const double* mats, si
     return QGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Adjoint sweep helpers
+// ---------------------------------------------------------------------------------------------
+bool is_rotation(int kind) {
+    return kind == QGPU_GATE_RX || kind == QGPU_GATE_RY || kind == QGPU_GATE_RZ ||
+           kind == QGPU_GATE_PHASE;
+}
+
+qgpu_op inverse_op(const qgpu_op& op) {
+    qgpu_op r = op;
+    switch (op.kind) {
+        case QGPU_GATE_S: r.kind = QGPU_GATE_SDAG; break;
+        case QGPU_GATE_SDAG: r.kind = QGPU_GATE_S; break;
+        case QGPU_GATE_T: r.kind = QGPU_GATE_TDAG; break;
+        case QGPU_GATE_TDAG: r.kind = QGPU_GATE_T; break;
+        case QGPU_GATE_X90: r.kind = QGPU_GATE_MX90; break;
+        case QGPU_GATE_MX90: r.kind = QGPU_GATE_X90; break;
+        case QGPU_GATE_Y90: r.kind = QGPU_GATE_MY90; break;
+        case QGPU_GATE_MY90: r.kind = QGPU_GATE_Y90; break;
+        case QGPU_GATE_RX: case QGPU_GATE_RY: case QGPU_GATE_RZ: case QGPU_GATE_PHASE:
+        case QGPU_GATE_CR:
+            r.param = -op.param;
+            break;
+        case QGPU_GATE_CRK:
+            r.kind = QGPU_GATE_CR;
+            r.param = -((2.0 * 3.14159265358979323846) / std::pow(2.0, (double)op.k));
+            break;
+        default:
+            break;  // H, X, Y, Z, CNot, CY, CZ, Swap, Toffoli are self-inverse
+    }
+    return r;
+}
+
+int pauli_run(const qgpu_op* ops, const std::vector<size_t>& gw, int n, PauliRun* out) {
+    const size_t k = gw.size();
+    std::vector<std::array<cd, 4>> fwd(k), inv(k);  // row-major 2x2: m[2 l + j]
+    for (size_t q = 0; q < k; ++q) {
+        LocalGate a, b;
+        int st = tabulate(ops[gw[q]], n, nullptr, 0, nullptr, 0, &a);
+        if (st == QGPU_OK) st = tabulate(inverse_op(ops[gw[q]]), n, nullptr, 0, nullptr, 0, &b);
+        if (st != QGPU_OK) return st;
+        for (int l = 0; l < 2; ++l)
+            for (int j = 0; j < 2; ++j) {
+                fwd[q][2 * l + j] = a.M[j * 2 + l];
+                inv[q][2 * l + j] = b.M[j * 2 + l];
+            }
+    }
+    auto mul = [](const std::array<cd, 4>& x, const std::array<cd, 4>& y) {
+        return std::array<cd, 4>{x[0] * y[0] + x[1] * y[2], x[0] * y[1] + x[1] * y[3],
+                                 x[2] * y[0] + x[3] * y[2], x[2] * y[1] + x[3] * y[3]};
+    };
+    // V runs over the later gates
+    std::array<cd, 4> undo{cd(1), cd(0), cd(0), cd(1)}, V{cd(1), cd(0), cd(0), cd(1)};
+    out->rots.clear();
+    for (int m = 0; m < 5; ++m) out->need[m] = false;
+    for (size_t q = 0; q < k; ++q) {  // q = 0 is the last gate of the run
+        undo = mul(inv[q], undo);
+        const qgpu_op& op = ops[gw[q]];
+        if (is_rotation(op.kind)) {
+            std::array<cd, 4> P{cd(0), cd(0), cd(0), cd(0)};
+            switch (op.kind) {
+                case QGPU_GATE_RX: P = {cd(0), cd(1), cd(1), cd(0)}; break;
+                case QGPU_GATE_RY: P = {cd(0), cd(0, -1), cd(0, 1), cd(0)}; break;
+                case QGPU_GATE_RZ: P = {cd(1), cd(0), cd(0), cd(-1)}; break;
+                default: P = {cd(-1), cd(0), cd(0), cd(-1)}; break;  // Phase: -I
+            }
+            const std::array<cd, 4> Vd{std::conj(V[0]), std::conj(V[2]), std::conj(V[1]),
+                                       std::conj(V[3])};
+            const std::array<cd, 4> Q = mul(mul(V, P), Vd);
+            std::array<double, 5> c{};  // kinds 1 X, 2 Y, 3 Z, 4 -I
+            c[1] = Q[2].real();
+            c[2] = Q[2].imag();
+            c[3] = 0.5 * (Q[0].real() - Q[3].real());
+            c[4] = -0.5 * (Q[0].real() + Q[3].real());
+            for (int m = 1; m <= 4; ++m) out->need[m] = out->need[m] || c[m] != 0.0;
+            out->rots.emplace_back(gw[q], c);
+        }
+        V = mul(V, fwd[q]);  // the gates after the next one back
+    }
+    out->undo = undo;
+    return QGPU_OK;
+}
+
 }  // namespace qgpu

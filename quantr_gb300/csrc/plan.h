@@ -3,6 +3,7 @@
 
 #include <stdint.h>
 
+#include <array>
 #include <complex>
 #include <string>
 #include <vector>
@@ -31,6 +32,26 @@ int op_arity(const qgpu_op& op, int n, int* k_out);
 // host-evaluated Custom table.
 int tabulate(const qgpu_op& op, int n, const double* mats, size_t n_mats, const uint8_t* none,
              size_t n_none, LocalGate* out);
+
+// Rotations (Rx, Ry, Rz, Phase: exp(-i theta P / 2) with P = X, Y, Z, -I), the gates with a
+// gradient.
+bool is_rotation(int kind);
+// The inverse of a non-Custom op as another op (U^dagger), quantr's conventions.
+qgpu_op inverse_op(const qgpu_op& op);
+
+// A run of single-wire gates on one wire undone by the adjoint sweep in one pass. A rotation
+// G = exp(-i theta P / 2) followed on its wire by V (the run's later gates) has gradient
+// Im <lambda| V P V^dag |phi>, taken before the run is undone; V P V^dag = q0 I + qx X + qy Y + qz Z
+// (real q: the product is Hermitian), so the gradient is a real combination of the sums
+// Im <lambda| s |phi> over s = X, Y, Z, -I.
+struct PauliRun {
+    std::array<cd, 4> undo;  // row-major 2x2: G_1^dag ... G_k^dag (G_k^dag applied first)
+    // per rotation: its op index and the coefficients of the sums (1 X, 2 Y, 3 Z, 4 -I)
+    std::vector<std::pair<size_t, std::array<double, 5>>> rots;
+    bool need[5] = {false, false, false, false, false};  // sums with a non-zero coefficient
+};
+// gw: the run's op indices into ops, in reverse order (gw[0] the run's last gate).
+int pauli_run(const qgpu_op* ops, const std::vector<size_t>& gw, int n, PauliRun* out);
 
 // ---------------------------------------------------------------------------------------------
 // Fused passes for the fast kernels (QGPU_MODE_FAST / QGPU_MODE_F64 / complex64).
