@@ -1432,4 +1432,46 @@ int pauli_run(const qgpu_op* ops, const std::vector<size_t>& gw, int n, PauliRun
     return QGPU_OK;
 }
 
+// Whether ops (applied in order) form an affine index map; if so, the gather tables of its
+// inverse: tabs[c * 256 + v] = xor of the inverse map's columns for the set bits of v (bits
+// 8c .. 8c+7), *d = inverse map of 0.
+bool affine_tables(const qgpu_op* ops, size_t n_ops, int n, std::vector<uint64_t>* tabs,
+                   uint64_t* d) {
+    for (size_t g = 0; g < n_ops; ++g) {
+        const int k = ops[g].kind;
+        if (k != QGPU_GATE_CNOT && k != QGPU_GATE_X && k != QGPU_GATE_SWAP) return false;
+    }
+    // inverse of g_m ... g_1 is g_1 ... g_m (each gate is an involution): apply ops last to first
+    auto inv = [&](uint64_t y) {
+        for (size_t g = n_ops; g-- > 0;) {
+            const qgpu_op& op = ops[g];
+            const int t = n - 1 - op.target;
+            if (op.kind == QGPU_GATE_X) {
+                y ^= 1ull << t;
+            } else if (op.kind == QGPU_GATE_CNOT) {
+                const int c = n - 1 - op.controls[0];
+                y ^= ((y >> c) & 1ull) << t;
+            } else {  // Swap
+                const int c = n - 1 - op.controls[0];
+                const uint64_t bt = (y >> t) & 1ull, bc = (y >> c) & 1ull;
+                if (bt != bc) y ^= (1ull << t) | (1ull << c);
+            }
+        }
+        return y;
+    };
+    *d = inv(0);
+    std::vector<uint64_t> col(n);
+    for (int b = 0; b < n; ++b) col[b] = inv(1ull << b) ^ *d;
+    const int nchunks = (n + 7) / 8;
+    tabs->assign((size_t)nchunks * 256, 0);
+    for (int c = 0; c < nchunks; ++c)
+        for (int v = 0; v < 256; ++v) {
+            uint64_t x = 0;
+            for (int k = 0; k < 8; ++k)
+                if (((v >> k) & 1) && 8 * c + k < n) x ^= col[8 * c + k];
+            (*tabs)[(size_t)c * 256 + v] = x;
+        }
+    return true;
+}
+
 }  // namespace qgpu

@@ -52,6 +52,11 @@ struct PauliRun {
 };
 // gw: the run's op indices into ops, in reverse order (gw[0] the run's last gate).
 int pauli_run(const qgpu_op* ops, const std::vector<size_t>& gw, int n, PauliRun* out);
+// Whether ops (CNot, X, Swap only), applied in order, form an affine index map y -> A y + b over
+// GF(2); if so, the gather tables of its inverse h for one out-of-place pass dst[y] = src[h(y)]:
+// h(y) = *d xor tabs[c * 256 + byte c of y] over the 8-bit chunks c of y.
+bool affine_tables(const qgpu_op* ops, size_t n_ops, int n, std::vector<uint64_t>* tabs,
+                   uint64_t* d);
 
 // ---------------------------------------------------------------------------------------------
 // Fused passes for the fast kernels (QGPU_MODE_FAST / QGPU_MODE_F64 / complex64).

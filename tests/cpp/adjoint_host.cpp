@@ -5,7 +5,9 @@
 //   * pauli_run: for random runs of single-wire gates (every one-wire kind, random angles), the
 //     undo matrix inverts the run, and each rotation's gradient formed from the Pauli sums
 //     Im <lambda| s |phi> (s = X, Y, Z, -I) with the run's coefficients equals the central
-//     difference of the energy <psi|H|psi> (random Hermitian H, random start state).
+//     difference of the energy <psi|H|psi> (random Hermitian H, random start state);
+//   * affine_tables: a run of CNot / X / Swap as one gather through 8-bit chunk tables equals
+//     the gates applied one by one.
 // Prints "fails <n>"; exit code 0 when there are none.
 #include <algorithm>
 #include <cmath>
@@ -173,6 +175,76 @@ int main() {
         }
     }
     std::printf("rotations %d, worst |gradient - central difference| %.3e\n", nrot, worst);
+
+    // affine_tables: random runs of CNot / X / Swap (n = 3..17, chunks of 8 bits, a partial last
+    // chunk); the one gather dst[y] = src[h(y)] equals the gates applied one by one through the
+    // library's tabulated images; runs with any other gate are refused
+    int gathers = 0;
+    for (int trial = 0; trial < 60; ++trial) {
+        const int n = 3 + trial % 15;
+        const uint64_t dim = 1ull << n;
+        std::vector<qgpu_op> ops;
+        const int len = 1 + (int)(rng() % 12);
+        for (int q = 0; q < len; ++q) {
+            const int t = (int)(rng() % n);
+            int c = (int)(rng() % (n - 1));
+            if (c >= t) ++c;
+            const int pick = (int)(rng() % 3);
+            ops.push_back(pick == 0 ? make_op(QGPU_GATE_X, t, {}, 0, 0)
+                                    : make_op(pick == 1 ? QGPU_GATE_CNOT : QGPU_GATE_SWAP, t, {c}, 0, 0));
+        }
+        std::vector<uint64_t> tabs;
+        uint64_t d = 0;
+        if (!qgpu::affine_tables(ops.data(), ops.size(), n, &tabs, &d)) {
+            ++fails;
+            continue;
+        }
+        std::vector<cd> src(dim), ref(dim), nx(dim);
+        for (uint64_t i = 0; i < dim; ++i) src[i] = cd((double)i, -0.5 * (double)i);
+        ref = src;
+        for (const qgpu_op& op : ops) {  // dense application of each gate's image
+            qgpu::LocalGate g;
+            if (qgpu::tabulate(op, n, nullptr, 0, nullptr, 0, &g) != QGPU_OK) std::exit(2);
+            const size_t kd = (size_t)1 << g.k;
+            std::vector<uint64_t> sc(kd);
+            uint64_t acting = 0;
+            for (size_t l = 0; l < kd; ++l) {
+                uint64_t off = 0;
+                for (int m = 0; m < g.k; ++m)
+                    if ((l >> (g.k - 1 - m)) & 1u) off |= 1ull << (n - 1 - g.wires[m]);
+                sc[l] = off;
+                acting |= off;
+            }
+            std::fill(nx.begin(), nx.end(), cd(0));
+            for (uint64_t b = 0; b < dim; ++b) {
+                if (b & acting) continue;
+                for (size_t j = 0; j < kd; ++j)
+                    for (size_t l = 0; l < kd; ++l) nx[b | sc[l]] += g.M[j * kd + l] * ref[b | sc[j]];
+            }
+            ref.swap(nx);
+        }
+        const int nch = (n + 7) / 8;
+        bool ok = tabs.size() == (size_t)nch * 256;
+        for (uint64_t y = 0; y < dim && ok; ++y) {
+            uint64_t x = d;
+            for (int c = 0; c < nch; ++c) x ^= tabs[(size_t)c * 256 + ((y >> (8 * c)) & 255u)];
+            ok = x < dim && src[x] == ref[y];
+        }
+        if (!ok) {
+            ++fails;
+            std::printf("affine_tables: run %d (n %d, %d gates) differs\n", trial, n, len);
+        }
+        ++gathers;
+    }
+    {
+        std::vector<qgpu_op> mixed = {make_op(QGPU_GATE_CNOT, 1, {0}, 0, 0), make_op(QGPU_GATE_TOFFOLI, 2, {0, 1}, 0, 0)};
+        std::vector<uint64_t> tabs;
+        uint64_t d = 0;
+        if (qgpu::affine_tables(mixed.data(), mixed.size(), 3, &tabs, &d)) ++fails;
+        mixed[1] = make_op(QGPU_GATE_H, 2, {}, 0, 0);
+        if (qgpu::affine_tables(mixed.data(), mixed.size(), 3, &tabs, &d)) ++fails;
+    }
+    std::printf("affine gathers %d\n", gathers);
     std::printf("fails %d\n", fails);
     return fails != 0;
 }
