@@ -461,6 +461,7 @@ struct Program {
 inline Program lower(const std::vector<Gate>& gates, size_t n, bool progress) {
     Program p;
     size_t counter = 0;
+    if (progress) std::cout << "Starting circuit simulation...\n";  // simulation.rs:32-34
     for (const Gate& g : gates) {
         if (g.kind == QGPU_GATE_ID) {
             ++counter;
@@ -488,9 +489,11 @@ inline Program lower(const std::vector<Gate>& gates, size_t n, bool progress) {
                 }
             }
         }
-        if (progress)
-            std::cout << "Applying gate " << g.kind << " on wire " << op.target << " # "
+        if (progress) {  // simulation.rs:183-200
+            std::cout << "Applying " << g.debug() << " on wire " << op.target << " # "
                       << counter + 1 << "/" << gates.size() << " \n";
+            if (counter + 1 == gates.size()) std::cout << "Finished circuit simulation.\n";
+        }
         p.ops.push_back(op);
         ++counter;
     }

@@ -6,6 +6,8 @@
 // Prints "<n> failure(s)".
 #include <cmath>
 #include <cstdio>
+#include <iostream>
+#include <sstream>
 #include <string>
 
 #include "quantr.hpp"
@@ -193,6 +195,24 @@ int main() {
     CHECK(error_of([] { Circuit::new_(2).add_gate(Gate::H(), 2); }) ==
           "The position, 2, is out of bounds for the circuit with 2 qubits.");
     CHECK(error_of([] { Circuit::new_(0); }) == "The initialised circuit must have at least one wire.");
+
+    // set_print_progress output while lowering (simulation.rs:32-34, 183-200): Id skipped, the
+    // gate printed with `{:?}`, the counter over every gate of the flat list
+    {
+        std::ostringstream log;
+        std::streambuf* old = std::cout.rdbuf(log.rdbuf());
+        quantr::lower({Gate::H(), Gate::Id(), Gate::CNot(0), Gate::Id(), Gate::Rz(0.5), Gate::Id()}, 3, true);
+        quantr::lower({Gate::Id(), Gate::X()}, 2, true);
+        std::cout.rdbuf(old);
+        CHECK(log.str() ==
+              "Starting circuit simulation...\n"
+              "Applying H on wire 0 # 1/6 \n"
+              "Applying CNot(0) on wire 2 # 3/6 \n"
+              "Applying Rz(0.5) on wire 1 # 5/6 \n"
+              "Starting circuit simulation...\n"
+              "Applying X on wire 1 # 2/2 \n"
+              "Finished circuit simulation.\n");
+    }
 
     std::printf("%d failure(s)\n", failures);
     return failures != 0;

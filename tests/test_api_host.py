@@ -194,3 +194,18 @@ def test_f64_in_messages_as_rust_prints_it():
     s = SuperPosition.new(2)
     assert _message(lambda: s.get_amplitude_from_state(ProductState([0, 1, 1]))).startswith(
         'Unable to retreive product state, |"011"> with dimension 3.')
+
+
+def test_progress_log_format(capsys):  # simulation.rs:32-34, 183-200
+    from quantr_gb300.circuit import _print_log
+
+    _print_log([Gate.H, Gate.Id, Gate.CNot(0), Gate.Id, Gate.Rz(0.5), Gate.Id], 3)
+    _print_log([Gate.Id, Gate.X], 2)
+    assert capsys.readouterr().out == (
+        "Starting circuit simulation...\n"
+        "Applying H on wire 0 # 1/6 \n"
+        "Applying CNot(0) on wire 2 # 3/6 \n"
+        "Applying Rz(0.5) on wire 1 # 5/6 \n"
+        "Starting circuit simulation...\n"
+        "Applying X on wire 1 # 2/2 \n"
+        "Finished circuit simulation.\n")
