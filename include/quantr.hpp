@@ -532,10 +532,11 @@ class SimulatedCircuit {
         std::map<ProductState, size_t> bins;
         for (size_t i = 0; i < nu; ++i)
             bins[ProductState::binary_basis(idx[i], num_qubits_)] = (size_t)cnt[i];
-        if (failed && !disable_warnings_)
-            std::cerr << "\x1b[93m[Quantr Warning] The superposition failed to collapse to a "
-                         "state during repeat measurements. This is likely due to the use of "
-                         "Gate::Custom where the mapping is not unitary.\x1b[0m\n";
+        if (!disable_warnings_)  // once per failed shot (add_to_bin, simulated_circuit.rs:116-130)
+            for (uint64_t f = 0; f < failed; ++f)
+                std::cerr << "\x1b[93m[Quantr Warning] The superposition failed to collapse to a "
+                             "state during repeat measurements. This is likely due to the use of "
+                             "Gate::Custom where the mapping is not unitary.\x1b[0m\n";
         return {true, std::move(bins)};
     }
     // simulated_circuit.rs:81-114. Shot 1 from the cached register, later shots from a
