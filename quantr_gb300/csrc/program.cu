@@ -1785,7 +1785,8 @@ __global__ void k_wait_selftest(uint32_t polls, int* err) {
 }
 
 extern "C" int qgpu_selftest_bounded_wait(qgpu_handle* h, uint32_t polls) {
-    if (!h || polls == 0 || polls > (1u << 20))
+    if (!h) return fail(QGPU_ERR_INVALID, "qgpu_selftest_bounded_wait: NULL handle");
+    if (polls == 0 || polls > (1u << 20))
         return fail(QGPU_ERR_INVALID, "qgpu_selftest_bounded_wait: polls must be 1..2^20");
     QGPU_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     k_wait_selftest<<<1, 32, 0, h->stream>>>(polls, h->d_err);

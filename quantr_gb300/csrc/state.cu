@@ -348,7 +348,9 @@ int qgpu_destroy(qgpu_handle* h) {
     return QGPU_OK;
 }
 
-int qgpu_num_qubits(const qgpu_handle* h) { return h ? h->n_qubits : QGPU_ERR_INVALID; }
+int qgpu_num_qubits(const qgpu_handle* h) {
+    return h ? h->n_qubits : fail(QGPU_ERR_INVALID, "qgpu_num_qubits: NULL handle");
+}
 
 int qgpu_set_mode(qgpu_handle* h, int mode) {
     if (!h) return fail(QGPU_ERR_INVALID, "qgpu_set_mode: NULL handle");

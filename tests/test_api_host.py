@@ -209,3 +209,50 @@ def test_progress_log_format(capsys):  # simulation.rs:32-34, 183-200
         "Starting circuit simulation...\n"
         "Applying X on wire 1 # 2/2 \n"
         "Finished circuit simulation.\n")
+
+
+def test_abi_rejects_null_handles_and_bad_sizes():
+    """Every entry point taking a handle returns QGPU_ERR_INVALID on NULL with a message naming
+    itself (qgpu_destroy(NULL) is a no-op, as free(NULL)); qgpu_create checks its size and
+    precision before touching a device. No call here reaches the GPU."""
+    lib = _native.load()
+    checked = 0
+    for name, (res, args) in _native._EXPORTS.items():
+        if not args or args[0] is not C.c_void_p:
+            continue
+        vals = [1 if a is C.c_uint32 else 0 if a in (C.c_int, C.c_size_t, C.c_uint64, C.c_double)
+                else None for a in args]
+        r = getattr(lib, name)(*vals)
+        if name == "qgpu_destroy":
+            assert r == 0
+        elif name == "qgpu_stream":
+            assert r is None
+        elif name == "qgpu_launch_count":
+            assert r == 0
+        else:
+            assert r == _native.QGPU_ERR_INVALID, name
+            assert lib.qgpu_last_error().decode().startswith(name + ":"), name
+            checked += 1
+    assert checked >= 18
+    h = C.c_void_p()
+    for n, prec in ((0, _native.QGPU_C128), (41, _native.QGPU_C128), (3, 7)):
+        assert lib.qgpu_create(n, prec, C.byref(h)) == _native.QGPU_ERR_INVALID
+        assert h.value is None
+    assert lib.qgpu_create(0, _native.QGPU_C128, C.byref(h)) == _native.QGPU_ERR_INVALID
+    assert b"1..40 qubits" in lib.qgpu_last_error()
+    assert lib.qgpu_create(3, _native.QGPU_C128, None) == _native.QGPU_ERR_INVALID
+
+
+def test_no_cpu_fallback_without_a_gpu():
+    """On a machine without a GPU the engine fails loudly: qgpu_create returns a CUDA error with
+    a message, and the Python API raises QuantrError instead of simulating on the host."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = _native.load()
+    h = C.c_void_p()
+    st = lib.qgpu_create(3, _native.QGPU_C128, C.byref(h))
+    assert st == _native.QGPU_ERR_CUDA and h.value is None
+    assert lib.qgpu_last_error()
+    with pytest.raises(QuantrError):
+        Circuit(2).add_gate(Gate.H, 0).simulate()
