@@ -1,9 +1,10 @@
 // pair_tc_host.cu — the arithmetic of k_pair2_tc emulated on the host with the library's own
 // image builder (quantr_gb300/csrc/pair_tc.cu): random 4x4 unitaries on all three bit layouts of
 // a tile, slot permutations folded before and after, tiles spread over 12 octaves of magnitude;
-// the 48-bit splitting, the 26 slice products of weight >= 4 (integer sums, as the tensor cores
-// accumulate them exactly), the recombination and the rescaling must reproduce the complex128
-// product within 1e-12 of the tile's largest amplitude. Needs no GPU; exit code 0 on success.
+// the 48-bit splitting (the kernel's own integer split, checked against round-to-nearest), the 26
+// slice products of weight >= 4 (integer sums, as the tensor cores accumulate them exactly), the
+// recombination and the rescaling must reproduce the complex128 product within 1e-12 of the
+// tile's largest amplitude. Needs no GPU; exit code 0 on success.
 #include "pair_tc.cu"
 
 namespace qgpu {
@@ -17,7 +18,7 @@ static float bf16_to_f(uint16_t b) { uint32_t u = (uint32_t)b << 16; float f; me
 int main() {
     std::mt19937_64 rng(7);
     std::normal_distribution<double> nd;
-    int fails = 0;
+    int fails = 0, split_fails = 0;
     for (int trial = 0; trial < 200; ++trial) {
         Plan plan;
         plan.pairs.resize(2);
@@ -73,7 +74,14 @@ int main() {
         for (int q = 0; q < 32; ++q) { uint32_t u; memcpy(&u, &h[q], 4); emax = std::max(emax, (int)((u >> 23) & 0xFF)); }
         const int k = 173 - emax;
         long long X[32];
-        for (int q = 0; q < 32; ++q) X[q] = std::llrint(std::ldexp((double)h[q], k)) + std::llrint(std::ldexp((double)l[q], k));
+        for (int q = 0; q < 32; ++q) {
+            X[q] = fixed48_bits(h[q], l[q], k);  // k_pair2_tc's own integer split
+            // against round-to-nearest in double (both parts are exact there): equal but at ties
+            for (float f : {h[q], l[q]}) {
+                const double e = std::ldexp((double)f, k), r = (double)scaled_int(f, k);
+                if (std::fabs(r - e) > 0.5 || (std::fabs(r - e) == 0.5 && std::fabs(r) < std::fabs(e))) ++split_fails;
+            }
+        }
         double out[32];
         for (int r = 0; r < 32; ++r) {
             double D[7] = {0};
@@ -99,6 +107,20 @@ int main() {
         if (err > 1e-12 * xmax) { ++fails; if (fails < 5) printf("trial %d err %.3e xmax %.3e\n", trial, err, xmax); }
         if (trial < 3) printf("trial %d rel err %.3e\n", trial, err / xmax);
     }
+    // the split's corner cases: exact ties (away from zero), the largest and smallest shifts
+    for (int k : {0, 1, 23, 24, 60, 150}) {
+        for (float f : {0.5f, -0.5f, 1.5f, -2.5f, 1.0f, 0x1.fffffep-1f, 0x1.8p-24f, 0x1.p-25f, 3.0e-38f}) {
+            const double e = std::ldexp((double)f, k);
+            if (std::fabs(e) >= 0x1p47) continue;
+            const double want = std::copysign(std::floor(std::fabs(e) + 0.5), e);
+            if ((double)scaled_int(f, k) != want) {
+                ++split_fails;
+                printf("scaled_int(%a, %d) = %lld, want %.0f\n", f, k, scaled_int(f, k), want);
+            }
+        }
+    }
+    printf("split fails %d\n", split_fails);
+    fails += split_fails;
     printf("fails %d\n", fails);
     return fails != 0;
 }
