@@ -244,12 +244,14 @@ class SuperPosition:
 
         if u is None:
             u = rng.next_f64()
-        c = 0.0
-        for i, a in enumerate(self.amplitudes):
-            c += a.real * a.real + a.imag * a.imag
-            if u < c:
-                return ProductState.binary_basis(i, self.product_dim)
-        return None
+        a = self.amplitudes
+        # the running sum in index order, one f64 add per amplitude as quantr's loop does
+        # (np.cumsum accumulates sequentially); the first i with u < c[i]
+        c = np.cumsum(a.real * a.real + a.imag * a.imag)
+        i = int(np.searchsorted(c, u, side="right"))
+        if i >= c.size:
+            return None
+        return ProductState.binary_basis(i, self.product_dim)
 
     def __iter__(self):  # super_position_iter.rs:56-72
         for i, a in enumerate(self.amplitudes):

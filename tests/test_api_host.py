@@ -256,3 +256,26 @@ def test_no_cpu_fallback_without_a_gpu():
     assert lib.qgpu_last_error()
     with pytest.raises(QuantrError):
         Circuit(2).add_gate(Gate.H, 0).simulate()
+
+
+def test_superposition_measure_is_the_crate_rule():  # super_positions.rs:332-342
+    """The first i with u < the running sum of |a_i|^2 (sequential f64 adds), None past the total;
+    checked against the literal loop, u on and next to every cumulative value."""
+    rng = np.random.default_rng(8)
+    for n in (1, 3, 6):
+        a = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        a[rng.random(a.size) < 0.3] = 0
+        a /= np.linalg.norm(a) * (1.0 if n != 3 else 1.2)  # n = 3: unnormalised, total < 1
+        sp = SuperPosition.new_with_amplitudes_unchecked(a)
+        cum, c = [], 0.0
+        for x in a:
+            c += x.real * x.real + x.imag * x.imag
+            cum.append(c)
+        us = list(rng.random(200)) + cum + [np.nextafter(v, 0) for v in cum] + [0.0, 0.999999]
+        for u in us:
+            want = next((i for i, v in enumerate(cum) if u < v), None)
+            got = sp.measure(u)
+            if want is None:
+                assert got is None
+            else:
+                assert got == ProductState.binary_basis(want, n)
