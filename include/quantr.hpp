@@ -164,6 +164,7 @@ class ProductState {
         return s;
     }
     bool operator==(const ProductState& o) const { return qubits == o.qubits; }
+    bool operator!=(const ProductState& o) const { return qubits != o.qubits; }
     bool operator<(const ProductState& o) const { return qubits < o.qubits; }
 };
 
@@ -336,6 +337,11 @@ class SuperPosition {
     };
     Iter begin() const { return {this, 0}; }
     Iter end() const { return {this, amplitudes.size()}; }
+    // #[derive(PartialEq)] (super_positions.rs:21): amplitudes and product dimension
+    bool operator==(const SuperPosition& o) const {
+        return product_dim == o.product_dim && amplitudes == o.amplitudes;
+    }
+    bool operator!=(const SuperPosition& o) const { return !(*this == o); }
 };
 
 // ---- gates (src/circuit/gate.rs:19-106) --------------------------------------------------------

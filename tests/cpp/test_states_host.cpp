@@ -121,6 +121,11 @@ int main() {
     for (int i = 0; i < shots; ++i) ones2 += m.measure().value().to_string() == "1";
     CHECK(ones == ones2);  // reseeding repeats the stream
 
+    // equality (derived PartialEq): amplitudes and dimension
+    CHECK(SuperPosition::new_with_hash_amplitudes(states) == SuperPosition::new_with_amplitudes({z, re, im, z}));
+    CHECK(SuperPosition::new_(2) != SuperPosition::new_with_amplitudes({z, re, im, z}));
+    CHECK(s01 != s10);
+
     // iteration over a superposition: (state, amplitude) in index order
     std::string seen;
     for (auto [st, a] : sp) seen += st.to_string() + (a == z ? "z " : "a ");
