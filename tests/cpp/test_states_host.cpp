@@ -9,6 +9,7 @@
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <unordered_map>
 
 #include "quantr.hpp"
 
@@ -125,6 +126,9 @@ int main() {
     CHECK(SuperPosition::new_with_hash_amplitudes(states) == SuperPosition::new_with_amplitudes({z, re, im, z}));
     CHECK(SuperPosition::new_(2) != SuperPosition::new_with_amplitudes({z, re, im, z}));
     CHECK(s01 != s10);
+    std::unordered_map<ProductState, int> hashed{{s01, 1}, {s10, 2}};  // derived Hash
+    CHECK(hashed.at(ProductState({Qubit::Zero, Qubit::One})) == 1 && hashed.size() == 2);
+    CHECK(std::hash<ProductState>()(s01) != std::hash<ProductState>()(s10));
 
     // iteration over a superposition: (state, amplitude) in index order
     std::string seen;
