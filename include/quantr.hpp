@@ -783,11 +783,13 @@ class Circuit {
 
 // #[derive(Hash)] on ProductState (product_states.rs:18): usable as an unordered_map key, as
 // quantr uses it in its HashMaps
+namespace std {
 template <>
-struct std::hash<quantr::ProductState> {
+struct hash<quantr::ProductState> {
     size_t operator()(const quantr::ProductState& p) const noexcept {
         uint64_t x = 0xcbf29ce484222325ull ^ (uint64_t)p.qubits.size();  // FNV-1a over the qubits
         for (quantr::Qubit q : p.qubits) x = (x ^ (uint64_t)q) * 0x100000001b3ull;
         return (size_t)x;
     }
 };
+}  // namespace std
