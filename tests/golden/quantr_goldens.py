@@ -59,6 +59,16 @@ def multicnot(num_control: int):
     return f
 
 
+def cccnot(input_state: ProductState):
+    """examples/custom_gate.rs:46-62: the CCC-not as a Custom function, None elsewhere."""
+    q = input_state.get_qubits()
+    if q == [Qubit.One, Qubit.One, Qubit.One, Qubit.Zero]:
+        return SuperPosition.from_(ProductState([Qubit.One] * 4))
+    if q == [Qubit.One] * 4:
+        return SuperPosition.from_(ProductState([Qubit.One, Qubit.One, Qubit.One, Qubit.Zero]))
+    return None
+
+
 def post_select(state_in: ProductState):
     """examples/post_select.rs:39-49: a non-unitary Custom map (no golden in the reference)."""
     if state_in.get_qubits()[0] == Qubit.Zero:

@@ -74,6 +74,23 @@ def test_non_unitary_post_select(oracle):
     assert np.allclose(out, expect, atol=1e-15)
 
 
+@pytest.mark.parametrize("engine", [0, 1], ids=["hashmap", "dense"])
+def test_examples_custom_multi_controlled_nots(oracle, engine):
+    """examples/custom_gate.rs (X on wires 0-2, then a Custom CCC-not on 3 with controls 0-2:
+    |1111>) and examples/generalised_control_not_gate.rs (X on all 6 wires, then a Custom
+    5-controlled not on wire 5: |111110>). Both Custom functions return None off their two
+    inputs, so every other amplitude keeps its value under the None rule."""
+    qc = Circuit(4)
+    qc.add_repeating_gate(Gate.X, [0, 1, 2]).add_gate(Gate.Custom(G.cccnot, [0, 1, 2], "X"), 3)
+    out = oracle.simulate(lower(qc.get_gates(), 4), engine=engine)
+    assert np.array_equal(out, np.eye(16, dtype=np.complex128)[0b1111])
+    qc = Circuit(6)
+    qc.add_repeating_gate(Gate.X, list(range(6))).add_gate(
+        Gate.Custom(G.multicnot(6), [0, 1, 2, 3, 4], "X"), 5)
+    out = oracle.simulate(lower(qc.get_gates(), 6), engine=engine)
+    assert np.array_equal(out, np.eye(64, dtype=np.complex128)[0b111110])
+
+
 def test_none_overwrite_rule(oracle):
     """A None input keeps its amplitude even when other inputs' images land on it
     (simulation.rs:120-133)."""
