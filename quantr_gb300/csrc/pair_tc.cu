@@ -26,7 +26,8 @@
 //
 // Status: correct (parity tests at 11-16 qubits; 30 qubits: norm drift 2.6e-14, checksum within
 // 1.4e-13 of the float-pair path) and 38 % fewer instructions than k_pair2, but slower on GB300
-// (13.2 against 11.4 ms per 30-qubit pass): with 16 warps per SM and the phases of a block in
+// (12.9 against 11.4 ms per 30-qubit pass, 13.2 before the split moved to the integer pipes):
+// with 16 warps per SM and the phases of a block in
 // sequence it is latency-bound (issue 33 %, tensor pipe 11 %, DRAM 31 %). A version that staged
 // the next block through cp.async was slower still (16.1 ms). It stays opt-in (QGPU_PAIR2_TC=1)
 // until the phases run warp-specialised and double-buffered.
