@@ -78,6 +78,11 @@ class ProductState:
         return v
 
     @staticmethod
+    def from_(value) -> "ProductState":
+        """`From<Qubit>` (product_states.rs:241-257): the one-qubit product state."""
+        return ProductState([Qubit(value)])
+
+    @staticmethod
     def binary_basis(index: int, basis_size: int) -> "ProductState":  # product_states.rs:205-215
         return ProductState([(index >> (basis_size - 1 - w)) & 1 for w in range(basis_size)])
 

@@ -279,3 +279,48 @@ def test_superposition_measure_is_the_crate_rule():  # super_positions.rs:332-34
                 assert got is None
             else:
                 assert got == ProductState.binary_basis(want, n)
+
+
+def test_crate_doc_examples_states():
+    """The assertions of the crate's rustdoc examples for the state types (product_states.rs,
+    product_states_iter.rs, qubit.rs, super_positions.rs, super_position_iter.rs, circuit.rs)."""
+    r = 2 ** -0.5
+    prod = ProductState([Qubit.One, Qubit.Zero])                       # product_states.rs:55-62
+    assert prod.get(1) == Qubit.Zero and prod.get(2) is None
+    assert prod.get_qubits() == [Qubit.One, Qubit.Zero]                 # :72-78
+    prod.get_mut_qubits()[1] = Qubit.One                                # :90-97
+    assert prod.get_qubits() == [Qubit.One, Qubit.One]
+    assert ProductState([Qubit.Zero, Qubit.One, Qubit.Zero]).num_qubits() == 3   # :127-133
+    p = ProductState([Qubit.One, Qubit.Zero, Qubit.One])                # :145-152
+    p.invert_digit(1)
+    assert p.get_qubits() == [Qubit.One, Qubit.One, Qubit.One]
+    assert ProductState([Qubit.Zero, Qubit.Zero]).kronecker_prod(Qubit.One).get_qubits() == \
+        [Qubit.Zero, Qubit.Zero, Qubit.One]                             # :170-178
+    assert str(ProductState([Qubit.Zero, Qubit.One])) == "01"           # :221-227
+    assert ProductState.from_(Qubit.One).get_qubits() == [Qubit.One]    # :245-251
+    assert list(ProductState([Qubit.One, Qubit.Zero, Qubit.Zero])) == \
+        [Qubit.One, Qubit.Zero, Qubit.Zero]                             # product_states_iter.rs:17-27
+    assert Qubit.Zero.kronecker_prod(Qubit.One).get_qubits() == [Qubit.Zero, Qubit.One]  # qubit.rs:27-33
+    s = SuperPosition.new(2)                                            # super_positions.rs:33-39
+    assert list(s.get_amplitudes()) == [1, 0, 0, 0]
+    assert list(SuperPosition.new_with_amplitudes([1, 0, 0, 0]).get_amplitudes()) == [1, 0, 0, 0]
+    h = SuperPosition.new_with_hash_amplitudes({ProductState([Qubit.Zero, Qubit.One]): 1.0})
+    assert list(h.get_amplitudes()) == [0, 1, 0, 0]                     # :96-103
+    assert SuperPosition.new_with_amplitudes([0, 1, 0, 0]).get_amplitude(1) == 1   # :137-143
+    assert s.get_num_qubits() == 2 and s.get_dimension() == 4           # :152-173
+    assert SuperPosition.new_with_amplitudes([0, 1, 0, 0]).get_amplitude_from_state(
+        ProductState([Qubit.Zero, Qubit.One])) == 1                     # :197-205
+    t = SuperPosition.new(2)
+    t.set_amplitudes([0, 1, 0, 0])                                      # :219-227
+    assert list(t.get_amplitudes()) == [0, 1, 0, 0]
+    u = SuperPosition.new(2)
+    u.set_amplitudes_from_states({ProductState([Qubit.Zero, Qubit.One]): 1.0})   # :259-268
+    assert list(u.get_amplitudes()) == [0, 1, 0, 0]
+    assert SuperPosition.new(2).to_hash_map() == {ProductState([Qubit.Zero, Qubit.Zero]): 1}  # :303-313
+    it = list(SuperPosition.new_with_amplitudes([0, r, r, 0]))          # super_position_iter.rs:18-37
+    assert it == [(ProductState([Qubit.Zero, Qubit.Zero]), 0), (ProductState([Qubit.Zero, Qubit.One]), r),
+                  (ProductState([Qubit.One, Qubit.Zero]), r), (ProductState([Qubit.One, Qubit.One]), 0)]
+    qc = Circuit(3)                                                     # circuit.rs:66-71, 94-101
+    assert qc.get_num_qubits() == 3
+    qc.add_gate(Gate.X, 2)
+    assert qc.get_gates() == [Gate.Id, Gate.Id, Gate.X]
