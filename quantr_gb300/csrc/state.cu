@@ -5,6 +5,7 @@
 // double2 {re, im} (16 B); complex64 is float2 (8 B). cudaMalloc gives 256-byte alignment, so
 // every 16/32-byte vector access used by the kernels is aligned.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -29,6 +30,14 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 int Scratch::ensure(size_t need) {
     if (need <= bytes) return QGPU_OK;
+    // Host-side fault injection: with QGPU_INJECT_SCRATCH_OOM=1 in the environment every scratch
+    // allocation fails as on a full device (the buffer held so far is kept), so that the error
+    // paths of the callers can be tested without any device fault. Read only when an allocation
+    // is due.
+    const char* inject = std::getenv("QGPU_INJECT_SCRATCH_OOM");
+    if (inject && inject[0] == '1')
+        return fail(QGPU_ERR_OOM, "device scratch allocation of " + std::to_string(need) +
+                                      " bytes failed (injected by QGPU_INJECT_SCRATCH_OOM)");
     if (ptr) cudaFree(ptr);
     ptr = nullptr;
     bytes = 0;

@@ -3,7 +3,8 @@
 Device side: the pipelined passes bound every mbarrier wait; here one CTA waits on a phase that
 nothing completes and must come back with QGPU_ERR_TIMEOUT, after which the same handle keeps
 working. Host side: bad requests (an oversize register, a bad op, a Custom gate in the adjoint)
-come back as error statuses, never as a device fault.
+and an injected allocation failure (QGPU_INJECT_SCRATCH_OOM) come back as error statuses, never
+as a device fault.
 """
 import numpy as np
 import pytest
@@ -30,3 +31,19 @@ def test_oversize_register_is_an_error_status(gpu_lib):
         nat.Handle(40)
     h = nat.Handle(3)  # later handles are unaffected
     assert h.download()[0] == 1
+
+
+def test_injected_scratch_oom_is_an_error_status_and_recoverable(gpu_lib, oracle, monkeypatch):
+    """Host-side fault injection: with QGPU_INJECT_SCRATCH_OOM=1 a scratch allocation fails as
+    on a full device. The call returns QGPU_ERR_OOM (raised as QuantrError), the register is
+    untouched, and once the variable is gone the same handle measures normally."""
+    prog = W.brickwork_qft(n=10, layers=2, seed=3)
+    h = nat.Handle(10)
+    h.apply(prog.ops, prog.mats, prog.none)
+    monkeypatch.setenv("QGPU_INJECT_SCRATCH_OOM", "1")
+    with pytest.raises(QuantrError, match="injected"):
+        h.measure(100, 7)  # a fresh handle's first measurement allocates its scratch
+    monkeypatch.delenv("QGPU_INJECT_SCRATCH_OOM")
+    idx, cnt, failed = h.measure(100, 7)
+    assert int(cnt.sum()) == 100 and failed == 0
+    assert np.max(np.abs(h.download() - oracle.simulate(prog, engine=oracle.DENSE))) <= 1e-12
