@@ -61,3 +61,29 @@ def test_two_rank_gather_matches_single_process(tmp_path):
     for r in range(2):
         e = np.load(tmp_path / f"e{r}.npy")
         assert np.allclose(e, ref, atol=1e-12, rtol=0)
+
+
+def test_shard_meets_the_list_scheduling_bound():
+    """Largest-first greedy sharding of uneven batches (10..24 qubits, as the batching
+    configuration draws them) over 1..8 ranks: every circuit exactly once, the heaviest rank at
+    most the average load plus one circuit, and no rank idle while circuits outnumber ranks."""
+    class _C:
+        def __init__(self, c):
+            self.c = c
+
+        def cost(self):
+            return self.c
+
+    rng = np.random.default_rng(4)
+    for trial in range(40):
+        count = int(rng.integers(1, 300))
+        cs = [_C(float(2 ** int(rng.integers(10, 25)) * int(rng.integers(20, 200))))
+              for _ in range(count)]
+        for world in range(1, 9):
+            parts = B.shard(cs, world)
+            assert len(parts) == world
+            assert sorted(i for p in parts for i in p) == list(range(count))
+            loads = [sum(cs[i].cost() for i in p) for p in parts]
+            assert max(loads) <= sum(loads) / world + max(c.cost() for c in cs)
+            if count >= world:
+                assert min(len(p) for p in parts) >= 1
