@@ -51,6 +51,9 @@ class Histogram(Mapping):
             yield ProductState.binary_basis(int(i), self.n)
 
     def __getitem__(self, key: ProductState) -> int:
+        # a key of another dimension is absent, as in the crate's HashMap (|101> is not |00101>)
+        if not isinstance(key, ProductState) or key.num_qubits() != self.n:
+            raise KeyError(key)
         j = np.searchsorted(self.indices, np.uint64(key.comp_basis()))
         if j < self.indices.size and int(self.indices[j]) == key.comp_basis():
             return int(self.counts[j])

@@ -324,3 +324,21 @@ def test_crate_doc_examples_states():
     assert qc.get_num_qubits() == 3
     qc.add_gate(Gate.X, 2)
     assert qc.get_gates() == [Gate.Id, Gate.Id, Gate.X]
+
+
+def test_histogram_behaves_as_the_crate_hashmap():
+    """measure_all's HashMap<ProductState, usize>, backed by the sampler's sorted arrays: lookups,
+    membership (keys of another dimension are absent), iteration, equality with a dict."""
+    from quantr_gb300.circuit import Histogram
+
+    h = Histogram(np.array([1, 5, 30], np.uint64), np.array([7, 2, 1], np.uint64), 5)
+    k5 = ProductState.binary_basis(5, 5)
+    assert len(h) == 3 and h[k5] == 2 and k5 in h
+    assert ProductState([1, 0, 1]) not in h          # |101>: 3 qubits, not |00101>
+    assert ProductState.binary_basis(4, 5) not in h and "00101" not in h
+    with pytest.raises(KeyError):
+        h[ProductState.binary_basis(2, 5)]
+    assert [str(k) for k in h] == ["00001", "00101", "11110"]
+    assert dict(h) == {ProductState.binary_basis(1, 5): 7, k5: 2, ProductState.binary_basis(30, 5): 1}
+    assert h == dict(h) and h.total() == 10
+    assert h.get(ProductState.binary_basis(3, 5), 0) == 0
