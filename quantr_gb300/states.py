@@ -57,7 +57,7 @@ class ProductState:
         return len(self.qubits)
 
     def invert_digit(self, place_num: int) -> "ProductState":
-        if place_num >= self.num_qubits():  # product_states.rs:154-166
+        if not 0 <= place_num < self.num_qubits():  # product_states.rs:154-166 (usize: no negatives)
             raise QuantrError(
                 f"The position of the binary digit, {place_num}, is out of bounds. The product "
                 f"dimension is {self.num_qubits()}, and so the position must be strictly less.")
