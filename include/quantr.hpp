@@ -673,12 +673,24 @@ class Circuit {
         return *this;
     }
 
+    // circuit.rs:324-341. A position beyond the register gets the out-of-bounds message of
+    // add_gates_with_positions (quantr's repeat scan indexes past its table and panics there).
     Circuit& add_repeating_gate(const Gate& g, const std::vector<size_t>& pos) {
         std::vector<bool> seen(num_qubits_, false);
+        bool repeated = false;
         for (size_t p : pos) {
-            if (p >= num_qubits_ || seen[p])
-                throw QuantrError("Attempted to add more than one gate onto a single wire.");
+            if (p >= num_qubits_)
+                throw QuantrError("The position, " + std::to_string(p) +
+                                  ", is out of bounds for the circuit with " +
+                                  std::to_string(num_qubits_) + " qubits.");
+            repeated = repeated || seen[p];
             seen[p] = true;
+        }
+        if (repeated) {
+            std::string list = "[";
+            for (size_t i = 0; i < pos.size(); ++i) list += (i ? ", " : "") + std::to_string(pos[i]);
+            throw QuantrError("Attempted to add more than one gate onto a single wire. The positions "
+                              "in " + list + "] must all differ.");
         }
         std::vector<Gate> col(num_qubits_, Gate::Id());
         for (size_t p : pos) col[p] = g;

@@ -125,7 +125,7 @@ class Circuit:
 
     def add_gates_with_positions(self, gates_with_positions: dict) -> "Circuit":
         for k in gates_with_positions:
-            if k >= self.num_qubits:
+            if not 0 <= k < self.num_qubits:  # (a usize in quantr: never negative)
                 raise QuantrError(f"The position, {k}, is out of bounds for the circuit with "
                                   f"{self.num_qubits} qubits.")
         gates = [gates_with_positions.get(r, Gate.Id) for r in range(self.num_qubits)]
@@ -145,7 +145,13 @@ class Circuit:
         return self
 
     def add_repeating_gate(self, gate: Gate, positions) -> "Circuit":
+        """circuit.rs:324-341. A position outside the register gets the out-of-bounds message of
+        add_gates_with_positions (quantr's repeat scan indexes past its table and panics there)."""
         positions = list(positions)
+        for p in positions:
+            if not 0 <= p < self.num_qubits:
+                raise QuantrError(f"The position, {p}, is out of bounds for the circuit with "
+                                  f"{self.num_qubits} qubits.")
         if self._contains_repeating_values(self.num_qubits, positions):
             raise QuantrError(f"Attempted to add more than one gate onto a single wire. The "
                               f"positions in {positions} must all differ.")
@@ -198,7 +204,7 @@ class Circuit:
             if nodes is None:
                 continue
             for node in nodes:
-                if node >= size:
+                if not 0 <= node < size:  # (a usize in quantr: never negative)
                     raise QuantrError(f"The control node at position {node}, is greater than the "
                                       f"umnber of qubits {size}.")
             if Circuit._contains_repeating_values(size, nodes):
@@ -211,7 +217,7 @@ class Circuit:
     def _contains_repeating_values(num_qubits: int, array) -> bool:
         seen = [False] * num_qubits
         for j in array:
-            if j >= num_qubits:
+            if not 0 <= j < num_qubits:
                 raise IndexError(j)
             if seen[j]:
                 return True

@@ -204,6 +204,12 @@ int main() {
     CHECK(error_of([] { Circuit::new_(2).add_gate(Gate::H(), 2); }) ==
           "The position, 2, is out of bounds for the circuit with 2 qubits.");
     CHECK(error_of([] { Circuit::new_(0); }) == "The initialised circuit must have at least one wire.");
+    CHECK(error_of([] { Circuit::new_(4).add_repeating_gate(Gate::X(), {0, 1, 1, 3}); }) ==
+          "Attempted to add more than one gate onto a single wire. The positions in [0, 1, 1, 3] "
+          "must all differ.");
+    CHECK(error_of([] { Circuit::new_(3).add_repeating_gate(Gate::H(), {0, 3}); }) ==
+          "The position, 3, is out of bounds for the circuit with 3 qubits.");
+    CHECK(Circuit::new_(3).add_repeating_gate(Gate::H(), {2, 0}).get_gates().size() == 3);
 
     // set_print_progress output while lowering (simulation.rs:32-34, 183-200): Id skipped, the
     // gate printed with `{:?}`, the counter over every gate of the flat list

@@ -342,3 +342,23 @@ def test_histogram_behaves_as_the_crate_hashmap():
     assert dict(h) == {ProductState.binary_basis(1, 5): 7, k5: 2, ProductState.binary_basis(30, 5): 1}
     assert h == dict(h) and h.total() == 10
     assert h.get(ProductState.binary_basis(3, 5), 0) == 0
+
+
+def test_builder_rejects_wires_outside_the_register():
+    """Positions and control nodes are usize in quantr: a negative one is rejected like one past
+    the register, never wrapped round to the last wire; repeated positions report the list."""
+    def msg(make):
+        with pytest.raises(QuantrError) as e:
+            make()
+        return e.value.message
+
+    assert msg(lambda: Circuit(3).add_gate(Gate.H, -1)) == \
+        "The position, -1, is out of bounds for the circuit with 3 qubits."
+    assert msg(lambda: Circuit(3).add_gate(Gate.CNot(-1), 0)) == \
+        "The control node at position -1, is greater than the umnber of qubits 3."
+    assert msg(lambda: Circuit(3).add_repeating_gate(Gate.H, [-1])).startswith("The position, -1,")
+    assert msg(lambda: Circuit(3).add_repeating_gate(Gate.H, [0, 3])).startswith("The position, 3,")
+    assert msg(lambda: Circuit(4).add_repeating_gate(Gate.X, [0, 1, 1, 3])) == \
+        "Attempted to add more than one gate onto a single wire. The positions in [0, 1, 1, 3] " \
+        "must all differ."
+    assert Circuit(3).add_repeating_gate(Gate.H, [2, 0]).get_gates() == [Gate.H, Gate.Id, Gate.H]
