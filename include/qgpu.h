@@ -160,8 +160,9 @@ int qgpu_measure_uniforms(qgpu_handle* h, const double* u, size_t n, int64_t* ou
  * in a fixed array inside the library's device image (about 1.5 MiB, held by every GPU that
  * loads the library until exit) and it calls no cudaMalloc/cudaFree. Limits: registers of at
  * most 24 qubits and at most 65536 uniforms per call; larger requests fail with
- * QGPU_ERR_INVALID. The first call on each device looks up the array's device address, so make
- * that call before any stream capture. All calls share the one array: calls that overlap on
+ * QGPU_ERR_INVALID. The first call on each device, and the first after that device's CUDA
+ * context was re-created (cudaDeviceReset), looks up the array's device address, so make that
+ * call before any stream capture. All calls share the one array: calls that overlap on
  * the GPU (other handles' streams on the same device) race. */
 int qgpu_measure_uniforms_noalloc(qgpu_handle* h, const double* u, size_t n, int64_t* out);
 

@@ -20,6 +20,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>  // CUcontext / CUresult types only; the driver is reached through the runtime
+
 #include "internal.cuh"
 
 namespace qgpu {
@@ -484,28 +486,78 @@ constexpr size_t NOALLOC_SCRATCH_BYTES =
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch per device. In host code the array's name is only a
-// host-side stand-in, so the address is looked up once per device with that device current.
+// Device address of g_noalloc_scratch. In host code the array's name is only a host-side
+// stand-in, so the address is looked up with the device current. A device's address belongs to
+// the CUDA context the library's module was loaded into: after a cudaDeviceReset (or any
+// teardown of the primary context) the next context loads the module again, possibly at another
+// address. So the cache is keyed on the device AND the current context's unique ID
+// (cuCtxGetId, fetched through the runtime's driver entry point so the library does not link
+// libcuda); a new context repeats the lookup. The lookup allocates nothing.
 constexpr int NOALLOC_MAX_DEVICES = 64;
-static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+struct NoallocSlot {
+    unsigned long long ctx_id = 0;  // 0: not looked up yet (context IDs start above 0)
+    void* ptr = nullptr;
+};
+static NoallocSlot g_noalloc_slot[NOALLOC_MAX_DEVICES];
 static std::mutex g_noalloc_mutex;
+
+using CtxGetCurrentFn = CUresult(CUDAAPI*)(CUcontext*);
+using CtxGetIdFn = CUresult(CUDAAPI*)(CUcontext, unsigned long long*);
+
+// ID of the context current on the calling thread (the device's primary context unless the
+// caller made another one current).
+static int current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        QGPU_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1));
+        QGPU_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return fail(QGPU_ERR_UNSUPPORTED,
+                        "qgpu_measure_uniforms_noalloc: driver has no cuCtxGetCurrent/cuCtxGetId");
+        get_current = (CtxGetCurrentFn)f1;
+        get_id = (CtxGetIdFn)f2;
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx)
+        return fail(QGPU_ERR_CUDA, "qgpu_measure_uniforms_noalloc: no current CUDA context");
+    if (get_id(ctx, id) != CUDA_SUCCESS)
+        return fail(QGPU_ERR_CUDA, "qgpu_measure_uniforms_noalloc: cuCtxGetId failed");
+    return QGPU_OK;
+}
 
 static int noalloc_scratch(int device, unsigned char** out) {
     if (device < 0 || device >= NOALLOC_MAX_DEVICES)
         return fail(QGPU_ERR_UNSUPPORTED, "qgpu_measure_uniforms_noalloc: device index " +
                                               std::to_string(device) + " out of range");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[device]) {
-        int cur = 0;
-        QGPU_CUDA(cudaGetDevice(&cur));
-        if (cur != device) QGPU_CUDA(cudaSetDevice(device));
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (cur != device) cudaSetDevice(cur);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        g_noalloc_ptr[device] = p;
+    int cur = 0;
+    QGPU_CUDA(cudaGetDevice(&cur));
+    if (cur != device) QGPU_CUDA(cudaSetDevice(device));
+    // The handle's creation initialised the device's context, so the query below finds it.
+    unsigned long long id = 0;
+    int st = current_context_id(&id);
+    void* p = nullptr;
+    if (st == QGPU_OK) {
+        NoallocSlot& slot = g_noalloc_slot[device];
+        if (slot.ptr && slot.ctx_id == id) {
+            p = slot.ptr;
+        } else {
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                st = cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            } else {
+                slot.ctx_id = id;
+                slot.ptr = p;
+            }
+        }
     }
-    *out = (unsigned char*)g_noalloc_ptr[device];
+    if (cur != device) cudaSetDevice(cur);
+    if (st != QGPU_OK) return st;
+    *out = (unsigned char*)p;
     return QGPU_OK;
 }
 

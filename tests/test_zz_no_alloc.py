@@ -42,6 +42,38 @@ def test_noalloc_sampler_matches_allocating_sampler(gpu_lib):
         h.close()
 
 
+@pytest.mark.parametrize("precision", [nat.QGPU_C128, nat.QGPU_C64])
+def test_noalloc_sampler_at_its_limits_and_on_none_shots(gpu_lib, precision):
+    """24 qubits (the largest register served, where the scan workspace is fullest) with the
+    largest uniform count, then a register whose total probability is 0.6, so that uniforms at
+    or above the total give None (-1); both precisions, two calls in a row each."""
+    lib = gpu_lib
+    rng = np.random.default_rng(77 + precision)
+    prog = W.random_columns(n=24, columns=6, seed=5)
+    h = nat.Handle(24, precision)
+    h.apply(prog.ops, prog.mats, prog.none)
+    u = rng.random(65536)
+    u[:8] = [0.0, 1e-300, 0.25, 0.5, 0.999999, np.nextafter(1.0, 0.0), 0.0, 0.5]
+    want = h.measure_uniforms(u)
+    st, got = _noalloc(lib, h, u)
+    assert st == nat.QGPU_OK, lib.qgpu_last_error()
+    assert np.array_equal(got, want)
+    h.close()
+
+    n = 14
+    amps = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    amps *= np.sqrt(0.6) / np.linalg.norm(amps)
+    h = nat.Handle(n, precision)
+    h.upload(amps)
+    u = np.concatenate([rng.random(4000), [0.6 - 1e-9, 0.6 + 1e-9, np.nextafter(1.0, 0.0)]])
+    want = h.measure_uniforms(u)
+    assert (want == -1).sum() > 1000 and (want >= 0).sum() > 1000
+    st, got = _noalloc(lib, h, u)
+    assert st == nat.QGPU_OK, lib.qgpu_last_error()
+    assert np.array_equal(got, want)
+    h.close()
+
+
 def test_noalloc_sampler_rejects_sizes_beyond_its_limits(gpu_lib):
     lib = gpu_lib
     h = nat.Handle(25)
