@@ -134,30 +134,85 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_reference_sample(n: int, budget_s: float, seed: int = 2) -> dict:
-    """The restated reference (oracle HashMap engine, single thread) on the first gates of the
-    same brickwork + QFT family at n qubits, run until budget_s elapses."""
+def host_cpu() -> dict:
+    """CPU model and core count of the host the CPU baseline runs on."""
+    model = None
+    try:
+        for line in open("/proc/cpuinfo"):
+            key = line.split(":")[0].strip().lower()
+            if key in ("model name", "cpu model", "hardware"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    if model is None:
+        try:  # Arm hosts: lscpu names the core type
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.strip().lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    import platform
+
+    return {"model": model or platform.processor() or "unknown", "arch": platform.machine(),
+            "nproc": os.cpu_count()}
+
+
+class PinnedToOneCore:
+    """Pins the calling thread to one core (by default the last allowed one) for a
+    single-threaded timing, as `taskset -c <core>` would, and restores the previous affinity
+    afterwards."""
+
+    def __init__(self, core: int | None = None):
+        self.want = core
+
+    def __enter__(self):
+        self.saved = None
+        self.core = None
+        if hasattr(os, "sched_getaffinity"):
+            self.saved = os.sched_getaffinity(0)
+            self.core = max(self.saved) if self.want is None else self.want
+            os.sched_setaffinity(0, {self.core})
+        return self
+
+    def __exit__(self, *exc):
+        if self.saved is not None:
+            os.sched_setaffinity(0, self.saved)
+
+
+def cpu_reference_sample(n: int, budget_s: float, seed: int = 2, layers: int = 20) -> dict:
+    """The restated reference (oracle HashMap engine, single thread pinned to one core) on the
+    first gates of the same brickwork + QFT family at n qubits, run until budget_s elapses (all
+    of the circuit when budget_s is None)."""
     from oracle import oracle as orc
     from quantr_gb300 import workloads as W
     from quantr_gb300.program import Program
 
-    prog = W.brickwork_qft(n=n, layers=20, seed=seed)
+    prog = W.brickwork_qft(n=n, layers=layers, seed=seed)
     state = np.zeros(1 << n, dtype=np.complex128)
     state[0] = 1.0
+    orc.lib()  # build/load outside the timed region
     done_bytes = 0.0
     gates = 0
     chunk = 16
-    t0 = time.perf_counter()
-    while gates < len(prog.ops) and time.perf_counter() - t0 < budget_s:
-        sub = Program(n, prog.ops[gates:gates + chunk], prog.mats, prog.none)
-        state = orc.simulate(sub, state, engine=orc.HASHMAP)
-        done_bytes += gate_bytes(sub)
-        gates += len(sub.ops)
-    dt = time.perf_counter() - t0
+    with PinnedToOneCore() as pin:
+        t0 = time.perf_counter()
+        while gates < len(prog.ops) and (budget_s is None or time.perf_counter() - t0 < budget_s):
+            sub = Program(n, prog.ops[gates:gates + chunk], prog.mats, prog.none)
+            state = orc.simulate(sub, state, engine=orc.HASHMAP)
+            done_bytes += gate_bytes(sub)
+            gates += len(sub.ops)
+        dt = time.perf_counter() - t0
+    cpu = host_cpu()
     return {"value": done_bytes / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"first {gates} of {len(prog.ops)} gates of the same brickwork+QFT family at "
-                      f"{n} qubits (restated reference HashMap engine, 1 thread, {dt:.1f} s)",
-            "seconds": dt, "gates": gates}
+                      f"{n} qubits (restated reference HashMap engine, 1 thread pinned to core "
+                      f"{pin.core}, {dt:.1f} s)",
+            "seconds": dt, "gates": gates, "total_gates": int(len(prog.ops)),
+            "seconds_per_gate": dt / max(1, gates), "cpu": cpu, "pinned_core": pin.core,
+            "state": state if gates == len(prog.ops) else None}
 
 
 def adjoint_leg(reps: int = 5, shift: bool = True) -> dict:
@@ -286,6 +341,82 @@ def run_batch_leg(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def _sweep_worker(job):
+    """One CPU-sweep entry in its own spawned process, pinned to one core: the restated
+    reference (HashMap engine, single-threaded) on a whole circuit."""
+    kind, n, core = job
+    from oracle import oracle as orc
+    from quantr_gb300 import workloads as W
+
+    with PinnedToOneCore(core):
+        if kind == "random_columns":
+            prog = W.random_columns(n=n, columns=40, seed=1)
+        else:
+            prog = W.brickwork_qft(n=n, layers=20, seed=2)
+        orc.lib()
+        t0 = time.perf_counter()
+        state = orc.simulate(prog, engine=orc.HASHMAP)
+        dt = time.perf_counter() - t0
+        out = {"workload": kind, "qubits": n, "gates": int(len(prog.ops)), "seconds": dt,
+               "seconds_per_gate": dt / len(prog.ops),
+               "amplitude_updates_per_s": gate_bytes(prog) / 32.0 / dt,
+               "gate_apply_gbs": gate_bytes(prog) / dt / 1e9, "core": core}
+        if kind == "random_columns":  # measure_all(1000): 1000 linear scans of the register
+            u = np.random.default_rng(1).random(1000)
+            t0 = time.perf_counter()
+            for x in u:
+                orc.measure_linear(state, float(x))
+            out["measure_all_1000_seconds"] = time.perf_counter() - t0
+    return out
+
+
+def run_cpu_sweep(args) -> None:
+    """CPU baseline sweep: the restated reference, single-threaded and pinned, on the 12-qubit
+    random-columns circuit in full (plus measure_all(1000)) and on the whole brickwork + QFT
+    circuit at n = 10, 12, ..., args.sweep_max qubits. Each circuit runs in its own process on its
+    own core, all at once (the largest n bounds the wall time). With a GPU present, the GPU's
+    fast and exact modes on the same circuits are timed beside them."""
+    import multiprocessing as mp
+
+    cores = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else \
+        list(range(os.cpu_count() or 1))
+    jobs = [("random_columns", 12)] + [("brickwork_qft", n)
+                                       for n in range(10, args.sweep_max + 1, 2)]
+    jobs = [(k, n, cores[(len(cores) - 1 - i) % len(cores)]) for i, (k, n) in enumerate(jobs)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(len(jobs)) as pool:
+        pending = pool.map_async(_sweep_worker, jobs)
+        gpu = sweep_gpu_points(args, jobs) if args.sweep_gpu else None
+        res = pending.get()
+    out = {"impl": "reference", "config": "cpu-sweep", "cpu": host_cpu(),
+           "threads_per_circuit": 1, "concurrent_circuits": len(jobs),
+           "wall_s": time.perf_counter() - t0, "results": res, "gpu": gpu}
+    print(json.dumps(out), flush=True)
+
+
+def sweep_gpu_points(args, jobs) -> list:
+    import torch
+
+    from quantr_gb300 import _native as nat
+    from quantr_gb300 import workloads as W
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    pts = []
+    for kind, n, _ in jobs:
+        prog = (W.random_columns(n=n, columns=40, seed=1) if kind == "random_columns"
+                else W.brickwork_qft(n=n, layers=20, seed=2))
+        pt = {"workload": kind, "qubits": n}
+        for name, mode in (("fast", nat.QGPU_MODE_FAST), ("exact", nat.QGPU_MODE_EXACT)):
+            h, ms, _ = timed_simulation(nat, n, prog, nat.QGPU_C128, mode, 3, 20, dev)
+            h.close()
+            pt[f"{name}_ms_per_circuit"] = ms
+            pt[f"{name}_gate_apply_gbs"] = gate_bytes(prog) / (ms / 1e3) / 1e9
+        pts.append(pt)
+    return pts
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -293,33 +424,146 @@ def dist_setup():
     return world, rank, local
 
 
+def _reference_worker(job):
+    """One host core's share of a reference-arm step (a spawned process): the restated
+    reference on the whole circuit, pinned to `core`."""
+    n, budget, core = job
+    with PinnedToOneCore(core):
+        r = cpu_reference_sample(n, budget_s=budget)
+    return {k: r[k] for k in ("value", "seconds", "gates", "total_gates")}
+
+
 def run_reference(args) -> None:
+    """The reference arm: quantr's simulate path (the restated reference, single-threaded as the
+    crate is) on every host core at once, one independent simulation of the same family at
+    args.ref_n qubits per core, each pinned to its core; value = the bytes all cores' gates move
+    (the same gate-equivalent GB/s) over the step's wall time."""
+    import multiprocessing as mp
+
     world, rank, _ = dist_setup()
     if rank != 0:
         return
     n = args.ref_n
-    for _ in range(args.warmup):
-        cpu_reference_sample(n, budget_s=0.5)
-    vals = []
-    samples = []
-    for _ in range(args.steps):
-        s = cpu_reference_sample(n, budget_s=args.ref_budget)
-        vals.append(s["value"])
-        samples.append(s)
+    cores = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else \
+        list(range(os.cpu_count() or 1))
+    ctx = mp.get_context("spawn")
+    vals, walls, per_core = [], [], []
+    with ctx.Pool(len(cores)) as pool:
+        for _ in range(args.warmup):
+            pool.map(_reference_worker, [(n, 0.5, c) for c in cores])
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_reference_worker, [(n, args.ref_budget, c) for c in cores])
+            wall = time.perf_counter() - t0
+            vals.append(sum(r["value"] * r["seconds"] for r in res) / wall)
+            walls.append(wall)
+            per_core.append(statistics.median(r["value"] for r in res))
     v = statistics.median(vals)
-    total_s = sum(s["seconds"] for s in samples)
+    cpu = host_cpu()
+    sample = (f"{len(cores)} independent single-threaded simulations of the brickwork+QFT family "
+              f"at {n} qubits ({res[0]['gates']} of {res[0]['total_gates']} gates each), one per "
+              f"host core, pinned; restated reference HashMap engine")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * total_s / max(1, args.steps), "higher_is_better": True,
+        "ms_per_step": 1e3 * statistics.mean(walls), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"brickwork+QFT {args.n}q c128 family, bounded sample at {n} qubits",
                    "qubits": n, "layers": 20, "seed": 2},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": samples[-1]["sample"]},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": len(cores), "kind": "port",
+                         "sample": sample, "cpu": cpu,
+                         "single_core_value": statistics.median(per_core)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def timed_simulation(nat, n, prog, precision, mode, warmup, steps, dev):
+    """Simulates `prog` from |0...0> on a fresh handle: `warmup` untimed runs, then `steps` runs
+    timed with CUDA events on the handle's stream, with per-pass profiling. Returns the handle
+    (holding the last result), ms per step and the per-kernel profile."""
+    import torch
+
+    h = nat.Handle(n, precision, mode)
+    stream = torch.cuda.ExternalStream(h.stream(), device=dev)
+    for _ in range(warmup):
+        h.set_zero()
+        h.apply(prog.ops, prog.mats, prog.none)
+    h.set_profiling(True)
+    h.profile(reset=True)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        h.set_zero()
+        h.apply(prog.ops, prog.mats, prog.none)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    return h, ev0.elapsed_time(ev1) / steps, h.profile(reset=True)
+
+
+def mode_summary(prof, ms, steps, gbytes, peak) -> dict:
+    pass_bytes = sum(v[2] for v in prof.values()) / steps
+    dom_name, (dl, dms, db) = max(prof.items(), key=lambda kv: kv[1][1])
+    dom_gbs = (db / dl) / (dms / dl / 1e3) / 1e9
+    return {"ms_per_step": ms, "value": gbytes / (ms / 1e3) / 1e9,
+            "pct_peak": (pass_bytes / (ms / 1e3) / 1e9) / peak,
+            "dominant_kernel": {"name": dom_name, "launches_per_step": dl / steps,
+                                "share_of_step": dms / steps / ms, "achieved_gbs": dom_gbs,
+                                "frac": dom_gbs / peak}}
+
+
+def reference_precision_leg(args, nat, prog, fast_handle, gbytes, peak, dev) -> dict:
+    """The same circuit in QGPU_MODE_F64 (native f64 FMA, the fast mode's plan) and in
+    QGPU_MODE_EXACT (one pass per gate, f64 products and sums in the reference's order: equal to
+    the oracle value for value), each timed, then compared on the device with the fast-mode
+    result: max |a_fast - a_exact|, max |a_f64 - a_exact|, 1 - fidelity and norm drift, without
+    downloading the 16 GiB registers."""
+    out = {}
+    hx, ms_x, prof_x = timed_simulation(nat, args.n, prog, nat.QGPU_C128, nat.QGPU_MODE_EXACT,
+                                        0, 1, dev)
+    out["exact"] = mode_summary(prof_x, ms_x, 1, gbytes, peak)
+    out["exact"].update({"steps": 1, "warmup": 0, "norm_drift": hx.norm() - 1.0})
+    hf, ms_f, prof_f = timed_simulation(nat, args.n, prog, nat.QGPU_C128, nat.QGPU_MODE_F64,
+                                        1, args.f64_steps, dev)
+    out["f64"] = mode_summary(prof_f, ms_f, args.f64_steps, gbytes, peak)
+    out["f64"].update({"steps": args.f64_steps, "warmup": 1, "norm_drift": hf.norm() - 1.0})
+    nx = hx.norm()
+    for name, h in (("fast", fast_handle), ("f64", hf)):
+        mx, inner = h.compare(hx)
+        nh = h.norm()
+        out.setdefault(name, {})
+        out[name]["vs_exact"] = {"max_abs_diff": mx,
+                                 "one_minus_fidelity": 1.0 - abs(inner) ** 2 / (nh * nx),
+                                 "tolerance": 1e-12, "within_tolerance": bool(mx <= 1e-12)}
+    hf.close()
+    hx.close()
+    return out
+
+
+def same_n_leg(args, nat, W, dev, sample) -> dict:
+    """The GPU arm on the CPU baseline's own size (the same family at args.ref_n qubits), so the
+    two numbers compare equal configurations; when the CPU sample ran the whole circuit, the
+    GPU's amplitudes are also compared with the restated reference's."""
+    n = args.ref_n
+    prog = W.brickwork_qft(n=n, layers=args.layers, seed=2)
+    gbytes = gate_bytes(prog)
+    out = {"qubits": n, "gates": int(len(prog.ops)), "cpu_value": sample["value"],
+           "cpu_gates_timed": sample["gates"], "unit": UNIT}
+    for name, mode in (("fast", nat.QGPU_MODE_FAST), ("exact", nat.QGPU_MODE_EXACT)):
+        h, ms, _ = timed_simulation(nat, n, prog, nat.QGPU_C128, mode, 3, 20, dev)
+        out[f"gpu_{name}"] = {"value": gbytes / (ms / 1e3) / 1e9, "ms_per_step": ms}
+        if sample.get("state") is not None:
+            a = h.download()
+            out[f"gpu_{name}"]["max_abs_diff_vs_cpu_reference"] = float(
+                np.max(np.abs(a - sample["state"])))
+            out[f"gpu_{name}"]["equal_to_cpu_reference"] = bool(np.array_equal(a, sample["state"]))
+        h.close()
+    out["note"] = ("CUDA events around 20 steps of set_zero + apply; the state (256 KiB) is "
+                   "L2-resident at this size")
+    return out
 
 
 def run_ours(args) -> None:
@@ -376,9 +620,15 @@ def run_ours(args) -> None:
     pass_bytes = sum(v[2] for v in prof.values()) / args.steps
     norm = h.norm()
     checksum = h.checksum()
+    peaks = measured_peaks()
+    precision_leg = None
+    if (not args.no_parity and world == 1 and precision == nat.QGPU_C128
+            and args.mode == "fast"):
+        precision_leg = reference_precision_leg(args, nat, prog, h, gbytes, peaks["hbm_gbs"], dev)
+        precision_leg["fast"].update(mode_summary(prof, ms_max, args.steps, gbytes,
+                                                  peaks["hbm_gbs"]))
     h.close()
 
-    peaks = measured_peaks()
     dom = max(prof.items(), key=lambda kv: kv[1][1])
     dom_name, (dom_launches, dom_ms, dom_bytes) = dom
     achieved = (dom_bytes / dom_launches) / (dom_ms / dom_launches / 1e3) / 1e9
@@ -451,9 +701,12 @@ def run_ours(args) -> None:
     if rank != 0:
         return
     cpu = None
+    same_n = None
     if world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_reference_sample(args.ref_n, budget_s=args.ref_budget)
-        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        sample = cpu_reference_sample(args.ref_n, budget_s=args.ref_budget)
+        cpu = {k: sample[k] for k in ("value", "unit", "cores", "kind", "sample", "cpu",
+                                      "seconds_per_gate")}
+        same_n = same_n_leg(args, nat, W, dev, sample)
     adjoint = None if (args.no_adjoint or world > 1) else adjoint_leg()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -466,10 +719,16 @@ def run_ours(args) -> None:
                                f"Rz Ry Rz + CNot bricks, {args.n}-qubit QFT + swaps",
                    "qubits": args.n, "gates": int(len(prog.ops)), "mode": args.mode,
                    "parallelism": f"replicas x{world}", "l2": "state 16 GiB > L2, no flush"},
+        "value_counts": ("gate-equivalent bytes: 2 x 16 B x the amplitudes each of the circuit's "
+                         "gates may change, per second (the bytes a gate-by-gate simulator such as "
+                         "quantr moves); fusion moves fewer, so this exceeds HBM. The bytes the "
+                         "passes really move are pct_peak x the measured HBM peak."),
         "pct_peak": (pass_bytes / (ms_max / 1e3) / 1e9) / peaks["hbm_gbs"],
+        "hbm_gbs_moved": pass_bytes / (ms_max / 1e3) / 1e9,
         "gates_per_s": len(prog.ops) / (ms_max / 1e3),
-        "roofline": roofline, "kernels": kernels,
-        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "adjoint": adjoint,
+        "roofline": roofline, "modes": precision_leg, "kernels": kernels,
+        "cpu_baseline": cpu, "same_n": same_n, "e2e": e2e, "gpu_launches": launches,
+        "adjoint": adjoint,
         "clocks": clocks.summary(),
         "result": {"norm": norm, "checksum": [checksum.real, checksum.imag]},
     }
@@ -492,11 +751,20 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--ref-n", type=int, default=14)
-    ap.add_argument("--ref-budget", type=float, default=15.0)
-    ap.add_argument("--config", choices=["headline", "precision", "batch", "adjoint"],
+    ap.add_argument("--ref-budget", type=float, default=40.0,
+                    help="seconds cap of the CPU sample (the whole 14-qubit circuit fits)")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the f64/exact timings and the on-device comparison with them")
+    ap.add_argument("--f64-steps", type=int, default=1)
+    ap.add_argument("--sweep-max", type=int, default=20,
+                    help="cpu-sweep config: largest brickwork+QFT size (even)")
+    ap.add_argument("--sweep-gpu", action="store_true",
+                    help="cpu-sweep config: also time the GPU on the same circuits")
+    ap.add_argument("--config", choices=["headline", "precision", "batch", "adjoint", "cpu-sweep"],
                     default="headline",
                     help="headline: the 30q c128 line; precision: 33q c64 / 32q c128; batch: "
-                         "4096 circuits of 10..24 qubits; adjoint: the differentiation leg alone")
+                         "4096 circuits of 10..24 qubits; adjoint: the differentiation leg alone; "
+                         "cpu-sweep: the restated reference on whole circuits at n = 10..")
     ap.add_argument("--adjoint-reps", type=int, default=5)
     ap.add_argument("--adjoint-no-shift", action="store_true",
                     help="adjoint config: skip the parameter-shift comparison")
@@ -514,6 +782,9 @@ def main() -> None:
         return
     if args.config == "batch":
         run_batch_leg(args)
+        return
+    if args.config == "cpu-sweep":
+        run_cpu_sweep(args)
         return
     if args.impl == "reference":
         run_reference(args)

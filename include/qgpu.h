@@ -178,6 +178,13 @@ int qgpu_extract_nonzero(qgpu_handle* h, double margin, uint64_t* idx_out, doubl
 int qgpu_norm(qgpu_handle* h, double* out);
 int qgpu_checksum(qgpu_handle* h, double* re_out, double* im_out);
 
+/* No counterpart in quantr (a parity check between two registers of the same size, e.g. one
+ * simulated in QGPU_MODE_FAST and one in QGPU_MODE_EXACT, without downloading either):
+ * *max_abs_diff = max_i |a_i - b_i| and (*inner_re, *inner_im) = sum_i conj(a_i) b_i, in f64 on
+ * the device (deterministic order). The precisions may differ. Waits for b's queued passes. */
+int qgpu_compare(qgpu_handle* a, qgpu_handle* b, double* max_abs_diff, double* inner_re,
+                 double* inner_im);
+
 /* ---- differentiation (no counterpart in quantr) ------------------------------------------
  * Observable H = sum_i a[i] Z_i Z_{(i+1) mod n} + sum_i b[i] X_i over the n wires (periodic),
  * a and b of length n. complex128 handles only. */

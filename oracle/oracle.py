@@ -17,6 +17,7 @@ LIB = HERE / "_build" / "liboracle.so"
 
 HASHMAP = 0  # literal HashMap-of-labels engine (the restated reference)
 DENSE = 1    # same accumulation order on flat arrays
+DENSE_PAR = 2  # the dense engine on all host cores (value for value equal to DENSE)
 
 _lib = None
 
@@ -27,7 +28,7 @@ def build(force: bool = False) -> Path:
         SRC.stat().st_mtime, (HERE.parent / "include" / "qgpu.h").stat().st_mtime)
     if force or stale:
         subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off",
-                        str(SRC), "-o", str(LIB)], check=True)
+                        "-pthread", str(SRC), "-o", str(LIB)], check=True)
     return LIB
 
 

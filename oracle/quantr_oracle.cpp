@@ -29,21 +29,27 @@
  *    caller: quantr draws it with `fastrand::f64()` (fastrand = "2.1.0", Cargo.toml:15), whose
  *    stream is not reproduced here.
  *
- * Two engines with identical arithmetic:
+ * Engines with identical arithmetic:
  *  - oracle_simulate_hashmap: the literal HashMap-of-labels algorithm (std::unordered_map
  *    keyed by a byte vector, one heap-allocated label per basis state and image entry). It is
  *    the restated reference timed as the CPU baseline.
  *  - oracle_simulate_dense: the same per-key accumulation order on flat arrays (no hashing),
  *    used for larger parity cases. Tests check that both engines agree value for value.
+ *  - a threaded form of the dense engine (independent groups of outputs on all host cores,
+ *    each output's products in the same order) for the 20-22 qubit parity cases; tests check
+ *    it against the dense engine value for value.
  *
  * Parity pinning: the restatement is checked against every amplitude golden of the crate's own
  * tests (src/circuit.rs:603-982, tests/qft.rs:30-39, tests/grovers.rs:124-133) and its layout
  * tests; the crate itself cannot be compiled here (no Rust toolchain).
  */
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -327,6 +333,81 @@ void apply_gate_dense(int n, const qgpu_op& op, const double* mats, const uint8_
     for (uint64_t i = 0; i < dim; ++i) reg[i] = state[i] ? out[i] : ZERO;
 }
 
+// ---------------------------------------------------------------------------------------
+// Engine 3: engine 2 on all host cores, value for value. An output t receives products only
+// from inputs that differ from t in the acting bits (its "group"), and engine 2 visits inputs
+// in increasing full index, so processing each group on its own, its members in increasing
+// full index, keeps every output's sequence of products and its None overwrite unchanged.
+// Groups are independent and are split across threads.
+// ---------------------------------------------------------------------------------------
+void apply_gate_dense_parallel(int n, const qgpu_op& op, const double* mats,
+                               const uint8_t* none_flags, std::vector<Cx>& reg, int threads) {
+    const int k = op_wires(op);
+    int pos[QGPU_MAX_OP_WIRES];
+    acting_positions(op, pos);
+    uint64_t bitmask[QGPU_MAX_OP_WIRES];
+    uint64_t acting = 0;
+    for (int m = 0; m < k; ++m) { bitmask[m] = 1ull << (n - 1 - pos[m]); acting |= bitmask[m]; }
+    const size_t kd = (size_t)1 << k;
+    std::vector<uint64_t> scatter(kd);  // local index -> offset of its acting bits
+    for (size_t l = 0; l < kd; ++l) {
+        uint64_t off = 0;
+        for (int m = 0; m < k; ++m)
+            if ((l >> (k - 1 - m)) & 1u) off |= bitmask[m];
+        scatter[l] = off;
+    }
+    // members of a group in increasing full index: local indices sorted by their offsets
+    std::vector<unsigned> visit(kd);
+    for (size_t l = 0; l < kd; ++l) visit[l] = (unsigned)l;
+    std::sort(visit.begin(), visit.end(),
+              [&](unsigned a, unsigned b) { return scatter[a] < scatter[b]; });
+    const uint64_t dim = (uint64_t)1 << n;
+    const uint64_t free_mask = (dim - 1) & ~acting;
+    const uint64_t groups = dim >> k;
+    auto work = [&](uint64_t g0, uint64_t g1) {
+        std::vector<Cx> img(kd), in(kd), out(kd);
+        std::vector<uint8_t> state(kd);
+        // base of group g0: deposit the bits of g0 into the free positions, low to high
+        uint64_t base = 0;
+        {
+            uint64_t rest = g0;
+            for (int b = 0; b < n && rest; ++b)
+                if ((free_mask >> b) & 1u) { if (rest & 1u) base |= 1ull << b; rest >>= 1; }
+        }
+        for (uint64_t g = g0; g < g1; ++g) {
+            for (size_t l = 0; l < kd; ++l) in[l] = reg[base | scatter[l]];
+            std::fill(state.begin(), state.end(), 0);
+            for (size_t v = 0; v < kd; ++v) {
+                const unsigned j = visit[v];  // input base|scatter[j], local index j
+                if (gate_image(op, j, mats, none_flags, img.data())) {
+                    for (size_t l = 0; l < kd; ++l) {
+                        Cx p = cmul(img[l], in[j]);
+                        if (state[l] == 1) out[l] = cadd(out[l], p);
+                        else if (state[l] == 0) { out[l] = p; state[l] = 1; }
+                    }
+                } else {
+                    out[j] = in[j];
+                    state[j] = 2;
+                }
+            }
+            for (size_t l = 0; l < kd; ++l) reg[base | scatter[l]] = state[l] ? out[l] : ZERO;
+            base = ((base | ~free_mask) + 1) & free_mask;  // next subset of the free bits
+        }
+    };
+    if (threads <= 1 || groups < 256) {
+        work(0, groups);
+        return;
+    }
+    std::vector<std::thread> pool;
+    const uint64_t per = (groups + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) {
+        const uint64_t g0 = t * per, g1 = std::min<uint64_t>(groups, g0 + per);
+        if (g0 >= g1) break;
+        pool.emplace_back(work, g0, g1);
+    }
+    for (auto& th : pool) th.join();
+}
+
 }  // namespace
 
 extern "C" {
@@ -334,7 +415,8 @@ extern "C" {
 const char* oracle_last_error(void) { return g_err.c_str(); }
 
 /* Simulates ops on `state` (interleaved re/im, 2^n amplitudes) in place. engine 0 = HashMap,
- * 1 = dense. Returns QGPU_OK or QGPU_ERR_INVALID. */
+ * 1 = dense, 2 = dense on all host cores (ORACLE_THREADS overrides the count). Returns QGPU_OK
+ * or QGPU_ERR_INVALID. */
 int oracle_simulate(int engine, int n, const qgpu_op* ops, size_t n_ops, const double* mats,
                     size_t n_mat_doubles, const uint8_t* none_flags, size_t n_none, double* state) {
     int st = validate(n, ops, n_ops, n_mat_doubles, n_none);
@@ -345,11 +427,18 @@ int oracle_simulate(int engine, int n, const qgpu_op* ops, size_t n_ops, const d
     std::vector<Cx> out;
     std::vector<uint8_t> flags;
     if (engine == 1) { out.resize(dim); flags.resize(dim); }
+    int threads = 1;
+    if (engine == 2) {
+        threads = (int)std::thread::hardware_concurrency();
+        if (const char* e = std::getenv("ORACLE_THREADS")) threads = std::atoi(e);
+        if (threads < 1) threads = 1;
+    }
     for (size_t g = 0; g < n_ops; ++g) {
         const qgpu_op& op = ops[g];
         if (op.kind <= QGPU_GATE_ID || op.kind >= QGPU_GATE_COUNT) continue;  // Identity skipped
         if (engine == 0) apply_gate_hashmap(n, op, mats, none_flags, reg);
-        else apply_gate_dense(n, op, mats, none_flags, reg, out, flags);
+        else if (engine == 1) apply_gate_dense(n, op, mats, none_flags, reg, out, flags);
+        else apply_gate_dense_parallel(n, op, mats, none_flags, reg, threads);
     }
     std::memcpy(state, reg.data(), dim * sizeof(Cx));
     return QGPU_OK;

@@ -68,6 +68,8 @@ _EXPORTS = {
     "qgpu_norm": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "qgpu_synchronize": (C.c_int, [C.c_void_p]),
     "qgpu_checksum": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "qgpu_compare": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
+                               C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "qgpu_expectation_zzx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "qgpu_adjoint_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
                                     C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
@@ -216,6 +218,13 @@ class Handle:
         re, im = C.c_double(), C.c_double()
         check(lib().qgpu_checksum(self._h, C.byref(re), C.byref(im)), "qgpu_checksum")
         return complex(re.value, im.value)
+
+    def compare(self, other: "Handle") -> tuple[float, complex]:
+        """(max_i |a_i - b_i|, sum_i conj(a_i) b_i) against another register, on the device."""
+        mx, re, im = C.c_double(), C.c_double(), C.c_double()
+        check(lib().qgpu_compare(self._h, other._h, C.byref(mx), C.byref(re), C.byref(im)),
+              "qgpu_compare")
+        return mx.value, complex(re.value, im.value)
 
     # ---- differentiation --------------------------------------------------------------------
     def expectation_zzx(self, a: np.ndarray, b: np.ndarray) -> float:

@@ -151,6 +151,59 @@ __global__ void k_reduce_final(const double2* __restrict__ partial, int nb, doub
     if (threadIdx.x == 0) *out = sh[0];
 }
 
+// Comparison of two registers of one size (qgpu_compare): per block the largest |a_i - b_i| and
+// the partial inner product sum conj(a_i) b_i over a fixed contiguous range, then one block
+// folds the partials (max, and fixed-tree sums), so the result is deterministic.
+template <class TA, class TB>
+__global__ void k_compare_partial(const TA* __restrict__ a, const TB* __restrict__ b,
+                                  uint64_t dim, uint64_t per_block, double4* __restrict__ partial) {
+    __shared__ double4 sh[RED_THREADS];
+    const uint64_t begin = blockIdx.x * per_block;
+    uint64_t end = begin + per_block;
+    if (end > dim) end = dim;
+    double mx = 0.0, re = 0.0, im = 0.0;
+    for (uint64_t i = begin + threadIdx.x; i < end; i += RED_THREADS) {
+        const double ar = (double)a[i].x, ai = (double)a[i].y;
+        const double br = (double)b[i].x, bi = (double)b[i].y;
+        const double dr = ar - br, di = ai - bi;
+        mx = fmax(mx, sqrt(dr * dr + di * di));
+        re = fma(ar, br, fma(ai, bi, re));
+        im = fma(ar, bi, fma(-ai, br, im));
+    }
+    sh[threadIdx.x] = make_double4(mx, re, im, 0.0);
+    __syncthreads();
+    for (int w = RED_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            sh[threadIdx.x].x = fmax(sh[threadIdx.x].x, sh[threadIdx.x + w].x);
+            sh[threadIdx.x].y += sh[threadIdx.x + w].y;
+            sh[threadIdx.x].z += sh[threadIdx.x + w].z;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_compare_final(const double4* __restrict__ partial, int nb, double4* out) {
+    __shared__ double4 sh[RED_THREADS];
+    double mx = 0.0, re = 0.0, im = 0.0;
+    for (int i = threadIdx.x; i < nb; i += RED_THREADS) {
+        mx = fmax(mx, partial[i].x);
+        re += partial[i].y;
+        im += partial[i].z;
+    }
+    sh[threadIdx.x] = make_double4(mx, re, im, 0.0);
+    __syncthreads();
+    for (int w = RED_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            sh[threadIdx.x].x = fmax(sh[threadIdx.x].x, sh[threadIdx.x + w].x);
+            sh[threadIdx.x].y += sh[threadIdx.x + w].y;
+            sh[threadIdx.x].z += sh[threadIdx.x + w].z;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
 int grid_for(const qgpu_handle* h, uint64_t work, int threads) {
     uint64_t blocks = (work + threads - 1) / threads;
     uint64_t cap = (uint64_t)h->sm_count * 16;
@@ -456,6 +509,50 @@ int qgpu_checksum(qgpu_handle* h, double* re_out, double* im_out) {
         *im_out = r.y;
     }
     return st;
+}
+
+int qgpu_compare(qgpu_handle* a, qgpu_handle* b, double* max_abs_diff, double* inner_re,
+                 double* inner_im) {
+    if (!a || !b || !max_abs_diff || !inner_re || !inner_im)
+        return fail(QGPU_ERR_INVALID, "qgpu_compare: NULL argument");
+    if (a->n_qubits != b->n_qubits)
+        return fail(QGPU_ERR_INVALID, "qgpu_compare: registers of " + std::to_string(a->n_qubits) +
+                                          " and " + std::to_string(b->n_qubits) + " qubits");
+    if (a->device != b->device)
+        return fail(QGPU_ERR_INVALID, "qgpu_compare: the registers live on different devices");
+    // b's queued passes finish before a's stream reads b.
+    QGPU_CUDA(cudaStreamSynchronize(b->stream));
+    const uint64_t dim = a->dim;
+    int nb = a->sm_count * 8;
+    if ((uint64_t)nb > dim) nb = (int)dim;
+    const uint64_t per_block = (dim + nb - 1) / nb;
+    int st = a->work.ensure(sizeof(double4) * (nb + 1));
+    if (st != QGPU_OK) return st;
+    double4* partial = (double4*)a->work.ptr;
+    const bool a64 = a->precision == QGPU_C128, b64 = b->precision == QGPU_C128;
+    if (a64 && b64)
+        k_compare_partial<double2, double2><<<nb, RED_THREADS, 0, a->stream>>>(
+            (const double2*)a->state, (const double2*)b->state, dim, per_block, partial);
+    else if (a64)
+        k_compare_partial<double2, float2><<<nb, RED_THREADS, 0, a->stream>>>(
+            (const double2*)a->state, (const float2*)b->state, dim, per_block, partial);
+    else if (b64)
+        k_compare_partial<float2, double2><<<nb, RED_THREADS, 0, a->stream>>>(
+            (const float2*)a->state, (const double2*)b->state, dim, per_block, partial);
+    else
+        k_compare_partial<float2, float2><<<nb, RED_THREADS, 0, a->stream>>>(
+            (const float2*)a->state, (const float2*)b->state, dim, per_block, partial);
+    QGPU_CHECK_LAUNCH("k_compare_partial");
+    k_compare_final<<<1, RED_THREADS, 0, a->stream>>>(partial, nb, partial + nb);
+    QGPU_CHECK_LAUNCH("k_compare_final");
+    a->launches += 2;
+    double4 r;
+    QGPU_CUDA(copy_async(a, &r, partial + nb, sizeof(double4), cudaMemcpyDeviceToHost));
+    QGPU_CUDA(cudaStreamSynchronize(a->stream));
+    *max_abs_diff = r.x;
+    *inner_re = r.y;
+    *inner_im = r.z;
+    return QGPU_OK;
 }
 
 }  // extern "C"

@@ -25,7 +25,9 @@ def test_reference_arm_prints_one_contract_line():
     assert line["higher_is_better"] is True and line["n_gpus"] == 1
     assert "workload" in line["config"]
     cb = line["cpu_baseline"]
-    assert cb["value"] == line["value"] and cb["cores"] == 1 and cb["kind"] in ("port", "reference")
+    # every host core runs one independent single-threaded simulation (quantr has no threads)
+    assert cb["value"] == line["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference")
+    assert cb["cpu"]["nproc"] >= cb["cores"] and cb["single_core_value"] > 0
     assert cb["unit"] == line["unit"] and cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}

@@ -83,13 +83,53 @@ def test_fused_modes_within_tolerance_cfg1(oracle, mode):
     assert np.max(np.abs(run_gpu(prog, mode) - ref)) <= TOL_FAST
 
 
-@pytest.mark.parametrize("mode", ["fast", "f64"])
-@pytest.mark.parametrize("n", [5, 11, 16])
+_BRICKWORK_REF = {}
+
+
+def _brickwork_ref(oracle, n):
+    """The oracle's amplitudes for the headline family at n qubits (threaded dense engine, equal
+    value for value to the dense engine), computed once per session."""
+    if n not in _BRICKWORK_REF:
+        prog = W.brickwork_qft(n=n, layers=20, seed=2)
+        _BRICKWORK_REF[n] = (prog, oracle.simulate(prog, engine=oracle.DENSE_PAR))
+    return _BRICKWORK_REF[n]
+
+
+@pytest.mark.parametrize("mode", ["fast", "f64", "exact"])
+@pytest.mark.parametrize("n", [5, 11, 16, 20, 22])
 def test_fused_modes_brickwork_qft(oracle, mode, n):
-    """The 30-qubit headline family at sizes the oracle finishes in seconds."""
-    prog = W.brickwork_qft(n=n, layers=20, seed=2)
-    ref = oracle.simulate(prog, engine=oracle.DENSE)
-    assert np.max(np.abs(run_gpu(prog, mode) - ref)) <= TOL_FAST
+    """The 30-qubit headline family (20 brickwork layers + QFT + swaps) against the oracle up to
+    22 qubits: fused modes within 1e-12 max-abs, exact mode value for value."""
+    prog, ref = _brickwork_ref(oracle, n)
+    out = run_gpu(prog, mode)
+    if mode == "exact":
+        assert np.array_equal(out, ref)
+    else:
+        assert np.max(np.abs(out - ref)) <= TOL_FAST
+
+
+def test_compare_registers_on_the_device(oracle):
+    """qgpu_compare (max |a - b| and <a|b> without a download) against the same figures from
+    downloaded amplitudes, for complex128 fast vs exact and complex128 vs complex64."""
+    prog, _ = _brickwork_ref(oracle, 16)
+    hs = [nat.Handle(16, p, m) for p, m in ((nat.QGPU_C128, nat.QGPU_MODE_FAST),
+                                            (nat.QGPU_C128, nat.QGPU_MODE_EXACT),
+                                            (nat.QGPU_C64, nat.QGPU_MODE_FAST))]
+    outs = []
+    for h in hs:
+        h.apply(prog.ops, prog.mats, prog.none)
+        outs.append(h.download())
+    for i, j in ((0, 1), (1, 0), (0, 2), (2, 1)):
+        mx, inner = hs[i].compare(hs[j])
+        want_mx = np.max(np.abs(outs[i] - outs[j]))
+        want_in = np.vdot(outs[i], outs[j])
+        assert abs(mx - want_mx) <= 1e-15 + 1e-12 * want_mx
+        assert abs(inner - want_in) <= 1e-12
+    assert hs[0].compare(hs[1])[0] <= TOL_FAST
+    with pytest.raises(QuantrError):
+        hs[0].compare(nat.Handle(15))
+    for h in hs:
+        h.close()
 
 
 @pytest.mark.parametrize("mode", ["exact", "fast", "f64"])

@@ -64,6 +64,44 @@ def test_engines_agree_value_for_value(oracle):
     assert np.array_equal(a, b)
 
 
+def _custom_heavy(n, seed):
+    """Rotations, CNot layers, a CRk row and Custom blocks with None entries (controls above and
+    below the target, a non-unitary one-wire block, a six-wire permutation)."""
+    rng = np.random.default_rng(seed)
+    b = ProgramBuilder(n)
+    for layer in range(3):
+        for w in range(n):
+            b.add("Ry", w, (), param=float(rng.uniform(0, 6.3)))
+        for w in range(layer % 2, n - 1, 2):
+            b.add("CNot", w + 1, (w,))
+        t, c1, c2 = (int(x) for x in rng.choice(n, size=3, replace=False))
+        blk = rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8))
+        b.add_custom(t, [c1, c2], blk / 3, (rng.random(8) < 0.25).astype(np.uint8))
+        b.add("H", 0)
+        for k in range(2, n + 1):
+            b.add("CRk", 0, (k - 1,), k=k)
+        b.add_custom(int(rng.integers(0, n)), [], np.array([[1.2, 0.1j], [0, 0.8]], np.complex128),
+                     np.array([0, layer % 2], np.uint8))
+        b.add("Toffoli", int(rng.integers(2, n)), (0, 1))
+    wires = [int(x) for x in rng.choice(n, size=6, replace=False)]
+    perm = np.eye(64, dtype=np.complex128)[rng.permutation(64)] * np.exp(1j * rng.random(64))[:, None]
+    b.add_custom(wires[2], wires[:2] + wires[3:], perm, (rng.random(64) < 0.2).astype(np.uint8))
+    return b.build()
+
+
+@pytest.mark.parametrize("threads", [3, 8])
+def test_threaded_dense_engine_equals_dense_engine(oracle, monkeypatch, threads):
+    """The threaded dense engine (used for the 20-22 qubit GPU parity cases) gives the dense
+    engine's values exactly: custom-heavy circuits with None entries at 14 qubits (enough groups
+    per gate for every thread), the brickwork + QFT family, and the 10-qubit sudoku."""
+    monkeypatch.setenv("ORACLE_THREADS", str(threads))
+    for prog in (_custom_heavy(14, 1), _custom_heavy(13, 2),
+                 W.brickwork_qft(n=14, layers=3, seed=2), lower(G.x3sudoko_circuit().get_gates(), 10)):
+        a = oracle.simulate(prog, engine=oracle.DENSE)
+        b = oracle.simulate(prog, engine=oracle.DENSE_PAR)
+        assert np.array_equal(a, b)
+
+
 def test_non_unitary_post_select(oracle):
     """examples/post_select.rs: Custom with a scaled |0> image and a zero image."""
     qc = Circuit(3)
