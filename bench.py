@@ -524,6 +524,9 @@ def reference_precision_leg(args, nat, prog, fast_handle, gbytes, peak, dev) -> 
     out = {}
     hx, ms_x, prof_x = timed_simulation(nat, args.n, prog, nat.QGPU_C128, nat.QGPU_MODE_EXACT,
                                         0, 1, dev)
+    if not prof_x:  # exact mode: one k_group pass per non-identity gate over the whole register
+        ng = int((prog.ops["kind"] != 0).sum())
+        prof_x = {"k_group": [ng, ms_x, ng * 32.0 * (1 << args.n)]}
     out["exact"] = mode_summary(prof_x, ms_x, 1, gbytes, peak)
     out["exact"].update({"steps": 1, "warmup": 0, "norm_drift": hx.norm() - 1.0})
     hf, ms_f, prof_f = timed_simulation(nat, args.n, prog, nat.QGPU_C128, nat.QGPU_MODE_F64,

@@ -25,7 +25,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contra
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", str(ROOT / "include")]
 
 CU_SOURCES = ["state.cu", "program.cu", "measure.cu", "adjoint.cu", "blocks.cu", "blocks_tc.cu",
-              "batch.cu", "pair_tc.cu"]
+              "batch.cu", "pair_tc.cu", "digits.cu"]
 CXX_SOURCES = ["plan.cpp"]
 
 

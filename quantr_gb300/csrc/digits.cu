@@ -1,0 +1,549 @@
+// digits.cu — complex128 double pair passes on the fifth-generation tensor cores in fixed-point
+// base-128 digits (the arithmetic is described in digits.cuh).
+//
+// Inside a run of pair passes the register stays in the digit layout; k_dg_from converts into it
+// (from complex128 or the resident float pairs) before the run and k_dg_to converts back after
+// it. A pass k_dg2 maps every 16-amplitude tile by one 16 x 16 complex matrix (two fused 4 x 4
+// blocks with the XOR terms around them folded in, or one block on two of the tile's bits): the
+// same work as k_pair2, which spends 364 FP32-pipe operations per amplitude on float-pair Dot2
+// sums. Here the products go to the tensor cores (49 digit-pair MMAs per tile, exact F32
+// accumulation) and the CUDA cores only permute bytes into BF16 operands (8 byte permutes per
+// amplitude) and run the carry chains (about 70 operations per amplitude).
+//
+// k_dg2: one CTA per SM, persistent over blocks of 128 tiles, warp-specialised:
+//   warp 0      lane 0 issues the MMAs: per block two chunks of 16 output reals, each 20 MMAs
+//               (M = 128 tiles, K = 16, N = 16..128) into one of three 160-column accumulators;
+//   warps 1-4   converters, one tile row each: load the tile's 16 slots (digit layout), byte-permute
+//               them into the A operand (K = 8 digits x 32 reals, BF16) of one of two buffers;
+//   warps 5-12  consumers, two groups of four warps, group g takes chunk g of every block: read the
+//               10 weights of its 16 outputs from tensor memory, run the carry chains, pack the
+//               digits and store the 8 amplitudes.
+// Hand-offs are mbarriers: a_full[2] (128 converter arrivals), a_empty[2] (MMA commit after a
+// block's second chunk), acc_full[3] (MMA commit), acc_empty[3] (128 consumer arrivals once their
+// tensor-memory loads completed). Every wait is bounded: a wait that runs out sets the error word
+// and an abort flag that stops every role; the MMA thread drains its MMAs (bounded) before the
+// CTA frees its tensor memory.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdlib>
+#include <cstring>
+
+#include "digits.cuh"
+#include "internal.cuh"
+#include "plan.h"
+#include "tc.cuh"
+
+namespace qgpu {
+
+constexpr int DG_M = 128;                               // tiles per block (MMA rows)
+constexpr int DG_THREADS = 416;                         // 13 warps
+constexpr int DG_K = 256;                               // A: 8 digits x 32 reals
+constexpr uint32_t DG_SBO_A = (DG_K / 8) * 128;         // 4096: 8-row groups of A
+constexpr uint32_t DG_A_BYTES = DG_M * DG_K * 2;        // 64 KB per buffer
+constexpr uint32_t DG_SBO_B = (32 / 8) * 128;           // 512: 8-row groups of B (K = 32)
+constexpr uint32_t DG_B_CHUNK = 128 * 32 * 2;           // 8 KB: rows 16 j + c (8 digits x 16 outputs)
+constexpr uint32_t DG_B_BYTES = 2 * DG_B_CHUNK;
+constexpr uint32_t DG_ACC_COLS = 16 * dg::NW;           // 160 columns per accumulator
+constexpr uint32_t DG_TCOLS = 512;
+constexpr size_t DG_SMEM = 2 * DG_A_BYTES + DG_B_BYTES + 1024;
+constexpr uint32_t DG_WAIT_LIMIT = 1u << 22;
+
+struct DgArgs {
+    uint64_t nblocks;                  // dim / 16 / 128
+    int bits[4];                       // tile bits, ascending (slot bit m <-> bits[m])
+    int* err;
+    int32_t kap[32][dg::KAP];          // carry constants per output real
+    uint32_t bimg[DG_B_BYTES / 4];     // matrix digits, both chunks, shared-memory layout
+};
+
+// ---- tensor-memory loads without the wait (the wait names the registers it completes) ------
+__device__ __forceinline__ void tm_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tm_wait(uint32_t (&r)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                   "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                   "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+                 :
+                 : "memory");
+}
+__device__ __forceinline__ void dg_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Consumer side of one chunk: the 10 weights of 16 output reals (8 amplitudes) from tensor
+// memory at taddr, carry chains, packed digit slots in out[]. Arrives on `release` once every
+// tensor-memory load completed.
+template <int G>
+__device__ __forceinline__ void dg_consume(uint32_t taddr, const DgArgs& a, uint32_t release,
+                                           uint4 (&out)[8]) {
+    uint32_t x[16], y[16];
+    float low[16];
+    int32_t tp[16];   // chain values of the previous (even) position
+    int32_t tc_[16];  // chain values of the current position
+    uint32_t wd[8][4];
+    tm_ld16(taddr + 0 * 16, x);   // D_5
+    tm_wait(x);
+    tm_ld16(taddr + 1 * 16, y);   // D_6 in flight
+#pragma unroll
+    for (int c = 0; c < 16; ++c) low[c] = __fadd_rn(__uint_as_float(x[c]), __uint_as_float((uint32_t)a.kap[16 * G + c][0]));
+    tm_wait(y);
+    tm_ld16(taddr + 2 * 16, x);   // D_7
+#pragma unroll
+    for (int c = 0; c < 16; ++c) low[c] = __fmaf_rn(__uint_as_float(y[c]), 128.0f, low[c]);
+    tm_wait(x);
+    tm_ld16(taddr + 3 * 16, y);   // D_8
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+        low[c] = __fmaf_rn(__uint_as_float(x[c]), 16384.0f, low[c]);
+        low[c] = __fmaf_rn(low[c], 1.0f / 2097152.0f, dg::MAGIC_F);
+    }
+    tm_wait(y);
+    tm_ld16(taddr + 4 * 16, x);   // D_9
+#pragma unroll
+    for (int c = 0; c < 16; ++c) tp[c] = dg::chain_first(__uint_as_float(y[c]), low[c], a.kap[16 * G + c][1]);
+    // positions 9..14: odd positions complete a word with the previous even one
+#pragma unroll
+    for (int p = 9; p <= 14; ++p) {
+        uint32_t(&cur)[16] = (p & 1) ? x : y;
+        uint32_t(&nxt)[16] = (p & 1) ? y : x;
+        tm_wait(cur);
+        if (p < 14) {
+            tm_ld16(taddr + (uint32_t)(p + 1 - dg::WMIN) * 16, nxt);
+        } else {  // every load of this accumulator completed: hand it back to the MMAs
+            tc::fence_before_sync();
+            dg_arrive(release);
+        }
+        if (p & 1) {
+#pragma unroll
+            for (int c = 0; c < 16; ++c) tc_[c] = dg::chain_next(__uint_as_float(cur[c]), tp[c], a.kap[16 * G + c][2 + p - 9]);
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                wd[u][(p - 9) / 2] = dg::out_word(tp[2 * u], tp[2 * u + 1], tc_[2 * u], tc_[2 * u + 1]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 16; ++c) tp[c] = dg::chain_next(__uint_as_float(cur[c]), tc_[c], a.kap[16 * G + c][2 + p - 9]);
+        }
+    }
+    // position 15 (no weight of its own) pairs with position 14 (in tp)
+#pragma unroll
+    for (int c = 0; c < 16; ++c) tc_[c] = a.kap[16 * G + c][8] + (tp[c] >> 7);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        wd[u][3] = dg::out_word(tp[2 * u], tp[2 * u + 1], tc_[2 * u], tc_[2 * u + 1]);
+        out[u] = make_uint4(wd[u][0], wd[u][1], wd[u][2], wd[u][3]);
+    }
+}
+
+__global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
+                                                       const __grid_constant__ DgArgs a) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    uint8_t* sA = sm;
+    uint8_t* sB = sm + 2 * DG_A_BYTES;
+    uint8_t* tail = sB + DG_B_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(tail);  // a_full[2] a_empty[2] acc_full[3] acc_empty[3] drain
+    uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 128);
+    int* abort_flag = reinterpret_cast<int*>(tail + 132);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t b_afull = smem_u32(bars), b_aempty = smem_u32(bars + 2),
+                   b_accfull = smem_u32(bars + 4), b_accempty = smem_u32(bars + 7),
+                   b_drain = smem_u32(bars + 10);
+
+    for (int i = tid; i < (int)(DG_B_BYTES / 4); i += DG_THREADS)
+        reinterpret_cast<uint32_t*>(sB)[i] = a.bimg[i];
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(b_afull + 8 * s, DG_M);
+            mbar_init(b_aempty + 8 * s, 1);
+        }
+        for (int s = 0; s < 3; ++s) {
+            mbar_init(b_accfull + 8 * s, 1);
+            mbar_init(b_accempty + 8 * s, DG_M);
+        }
+        mbar_init(b_drain, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tc::alloc(smem_u32(slot), DG_TCOLS);
+    fence_proxy_async_shared();  // B (generic-proxy writes) visible to the MMAs
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint64_t nmine =
+        (a.nblocks > blockIdx.x) ? (a.nblocks - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t o0 = 1ull << a.bits[0], o1 = 1ull << a.bits[1], o2 = 1ull << a.bits[2],
+                   o3 = 1ull << a.bits[3];
+    auto slot_off = [&](int j) {
+        return ((j & 1) ? o0 : 0) | ((j & 2) ? o1 : 0) | ((j & 4) ? o2 : 0) | ((j & 8) ? o3 : 0);
+    };
+    auto tile_base = [&](uint64_t blk, int r) {
+        return insert_zero(
+            insert_zero(insert_zero(insert_zero(blk * DG_M + r, a.bits[0]), a.bits[1]), a.bits[2]),
+            a.bits[3]);
+    };
+    auto fail_now = [&](int code) {
+        atomicExch(a.err, code);
+        atomicExch(abort_flag, 1);
+    };
+    auto aborted = [&]() { return *(volatile int*)abort_flag != 0; };
+
+    if (warp == 0) {  // ------------------------------------------------------------ MMA issue
+        if (lane == 0) {
+            bool issued = false;
+            for (uint64_t t = 0; t < 2 * nmine; ++t) {
+                const uint64_t it = t >> 1;
+                const int q = (int)(t & 1), s = (int)(it & 1), ai = (int)(t % 3);
+                if (q == 0 && !mbar_wait_bounded(b_afull + 8 * s, (uint32_t)((it >> 1) & 1), DG_WAIT_LIMIT)) {
+                    fail_now(5);
+                    break;
+                }
+                if (t >= 3 && !mbar_wait_bounded(b_accempty + 8 * ai, (uint32_t)(((t / 3) - 1) & 1),
+                                                  DG_WAIT_LIMIT)) {
+                    fail_now(6);
+                    break;
+                }
+                if (aborted()) break;
+                tc::fence_after_sync();
+                const uint32_t sa = smem_u32(sA + (uint32_t)s * DG_A_BYTES);
+                const uint32_t sb = smem_u32(sB + (uint32_t)q * DG_B_CHUNK);
+                const uint32_t acc = tmem + DG_ACC_COLS * (uint32_t)ai;
+#pragma unroll
+                for (int k = 0; k < dg::NSTEPS; ++k) {
+                    const dg::MmaStep ms = dg::mma_step(k);
+                    const uint32_t idesc = tc::idesc_bf16(DG_M, 16 * (ms.jend - ms.jmin));
+#pragma unroll
+                    for (int kk = 0; kk < 2; ++kk) {
+                        const uint64_t ad = tc::smem_desc(sa + (uint32_t)(4 * ms.i + 2 * kk) * 128, 128, DG_SBO_A);
+                        const uint64_t bd =
+                            tc::smem_desc(sb + (uint32_t)ms.jmin * 1024 + (uint32_t)kk * 256, 128, DG_SBO_B);
+                        tc::mma_bf16(acc + (uint32_t)(16 * (ms.i + ms.jmin - dg::WMIN)), ad, bd, idesc,
+                                     (ms.init && kk == 0) ? 0u : 1u);
+                    }
+                }
+                issued = true;
+                tc::commit(b_accfull + 8 * ai);
+                if (q == 1) tc::commit(b_aempty + 8 * s);
+            }
+            if (issued) {  // every MMA completed before the tensor memory is freed
+                tc::commit(b_drain);
+                if (!mbar_wait_bounded(b_drain, 0, DG_WAIT_LIMIT)) atomicExch(a.err, 7);
+            }
+        }
+        __syncwarp();
+    } else if (warp <= 4) {  // ------------------------------------------------------ converters
+        const int r = tid - 32;
+        uint4 v[16];
+        if (nmine > 0) {
+            const uint64_t b0 = tile_base(blockIdx.x, r);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = st[b0 | slot_off(j)];
+        }
+        for (uint64_t it = 0; it < nmine; ++it) {
+            const int s = (int)(it & 1);
+            if (it >= 2 && !mbar_wait_bounded(b_aempty + 8 * s, (uint32_t)(((it >> 1) - 1) & 1), DG_WAIT_LIMIT)) {
+                fail_now(8);
+                break;
+            }
+            if (aborted()) break;
+            uint8_t* A = sA + (uint32_t)s * DG_A_BYTES;
+#pragma unroll
+            for (int i = 0; i < dg::DIGITS; ++i) {
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    uint32_t w[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const uint4 s4 = v[4 * g + q];
+                        const uint32_t sw = (i >> 1) == 0 ? s4.x : (i >> 1) == 1 ? s4.y : (i >> 1) == 2 ? s4.z : s4.w;
+                        w[q] = dg::a_word(sw, i & 1);
+                    }
+                    *reinterpret_cast<uint4*>(A + dg::op_off(r, 32 * i + 8 * g, DG_SBO_A)) =
+                        make_uint4(w[0], w[1], w[2], w[3]);
+                }
+            }
+            fence_proxy_async_shared();  // the generic-proxy writes of A visible to the MMAs
+            dg_arrive(b_afull + 8 * s);
+            if (it + 1 < nmine) {  // the next block's loads fly while this one waits
+                const uint64_t bn = tile_base(blockIdx.x + (it + 1) * gridDim.x, r);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = st[bn | slot_off(j)];
+            }
+        }
+    } else {  // ------------------------------------------------------------------- consumers
+        const int g = (warp - 5) >> 2;
+        const int quad = warp & 3;
+        const int r = 32 * quad + lane;
+        for (uint64_t it = 0; it < nmine; ++it) {
+            const uint64_t t = 2 * it + (uint64_t)g;
+            const int ai = (int)(t % 3);
+            if (!mbar_wait_bounded(b_accfull + 8 * ai, (uint32_t)((t / 3) & 1), DG_WAIT_LIMIT)) {
+                fail_now(9);
+                break;
+            }
+            if (aborted()) break;
+            tc::fence_after_sync();
+            const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + DG_ACC_COLS * (uint32_t)ai;
+            uint4 out[8];
+            if (g == 0) dg_consume<0>(taddr, a, b_accempty + 8 * ai, out);
+            else dg_consume<1>(taddr, a, b_accempty + 8 * ai, out);
+            const uint64_t base = tile_base(blockIdx.x + it * gridDim.x, r);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) st[base | slot_off(8 * g + u)] = out[u];
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::dealloc(tmem, DG_TCOLS);
+}
+
+// ---- layout conversions -----------------------------------------------------------------------
+// x (f64) -> round(x 2^sx) from the double's bits (integer pipes), clamped to |X| <= 2^54 (a value
+// outside that range sets the error word: the host's bound on the amplitudes was wrong).
+__device__ __forceinline__ long long dg_fixed_f64(double x, int sx, int* err) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FFu);
+    if (e == 0) return 0;  // zero or subnormal
+    const long long m = (long long)((b & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+    const int sh = e - 1075 + sx;
+    long long v;
+    if (sh > 2) {
+        v = dg::XMAX + 1;
+    } else if (sh >= 0) {
+        v = m << sh;
+    } else if (sh >= -60) {
+        v = (m + (1ll << (-sh - 1))) >> (-sh);
+    } else {
+        v = 0;
+    }
+    if (v > dg::XMAX) {
+        v = dg::XMAX;
+        atomicExch(err, 10);
+    }
+    return (b >> 63) ? -v : v;
+}
+// the float pair h + l times 2^sx, rounded (integer pipes)
+__device__ __forceinline__ long long dg_scaled_f32(float x, int sx) {
+    const uint32_t b = __float_as_uint(x);
+    const int e = (int)((b >> 23) & 0xFFu);
+    if (e == 0) return 0;
+    const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
+    const int sh = e - 150 + sx;
+    long long v;
+    if (sh > 31) v = dg::XMAX + 1;
+    else if (sh >= 0) v = m << sh;
+    else if (sh >= -30) v = (m + (1ll << (-sh - 1))) >> (-sh);
+    else v = 0;
+    return (b >> 31) ? -v : v;
+}
+__device__ __forceinline__ long long dg_clamp(long long v, int* err) {
+    if (v > dg::XMAX || v < -dg::XMAX) {
+        atomicExch(err, 10);
+        v = v > 0 ? dg::XMAX : -dg::XMAX;
+    }
+    return v;
+}
+
+// from = 0: complex128 -> digits; from = 1: resident float pairs -> digits
+template <int FROM>
+__global__ void k_dg_from(uint4* __restrict__ st, uint64_t dim, int sx, int* err) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (; i < dim; i += stride) {
+        const uint4 v = st[i];
+        long long xr, xi;
+        if (FROM == 0) {
+            xr = dg_fixed_f64(__hiloint2double((int)v.y, (int)v.x), sx, err);
+            xi = dg_fixed_f64(__hiloint2double((int)v.w, (int)v.z), sx, err);
+        } else {  // (re_h, im_h | re_l, im_l)
+            xr = dg_clamp(dg_scaled_f32(__uint_as_float(v.x), sx) + dg_scaled_f32(__uint_as_float(v.z), sx), err);
+            xi = dg_clamp(dg_scaled_f32(__uint_as_float(v.y), sx) + dg_scaled_f32(__uint_as_float(v.w), sx), err);
+        }
+        uint32_t w[4];
+        dg::pack_digits((uint64_t)(xr + dg::OFFSET), (uint64_t)(xi + dg::OFFSET), w);
+        st[i] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// to = 0: digits -> complex128; to = 1: digits -> resident float pairs
+template <int TO>
+__global__ void k_dg_to(uint4* __restrict__ st, uint64_t dim, int sx) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const double scale = ldexp(1.0, -sx);
+    for (; i < dim; i += stride) {
+        const uint4 v = st[i];
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+        uint64_t ur, ui;
+        dg::unpack_digits(w, ur, ui);
+        const long long xr = (long long)ur - dg::OFFSET, xi = (long long)ui - dg::OFFSET;
+        if (TO == 0) {
+            const double re = __ll2double_rn(xr) * scale, im = __ll2double_rn(xi) * scale;
+            st[i] = make_uint4((uint32_t)__double2loint(re), (uint32_t)__double2hiint(re),
+                               (uint32_t)__double2loint(im), (uint32_t)__double2hiint(im));
+        } else {
+            // X = H + L with H = X rounded to 24 bits (exact as a float) and L = X - H
+            const float hr = __ll2float_rn(xr), hi = __ll2float_rn(xi);
+            const float lr = __ll2float_rn(xr - __float2ll_rn(hr)), li = __ll2float_rn(xi - __float2ll_rn(hi));
+            const float fs = (float)scale;  // a power of two within the float range
+            float rh = hr * fs, ih = hi * fs, rl = lr * fs, il = li * fs;
+            // the float pairs flush magnitudes below 2^-126 (as split_f64 does)
+            if ((__float_as_uint(rh) & 0x7F800000u) == 0) rh = rl = 0.0f;
+            if ((__float_as_uint(ih) & 0x7F800000u) == 0) ih = il = 0.0f;
+            if ((__float_as_uint(rl) & 0x7F800000u) == 0) rl = 0.0f;
+            if ((__float_as_uint(il) & 0x7F800000u) == 0) il = 0.0f;
+            st[i] = make_uint4(__float_as_uint(rh), __float_as_uint(ih), __float_as_uint(rl),
+                               __float_as_uint(il));
+        }
+    }
+}
+
+// ---- host side ----------------------------------------------------------------------------------
+namespace {
+
+uint16_t dg_bf16(int v) {  // |v| <= 256: exact in BF16
+    const float f = (float)v;
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return (uint16_t)(u >> 16);
+}
+
+}  // namespace
+
+// The pass's 16 x 16 complex matrix (M[out slot][in slot], physical slots) as the B operand's
+// digits and the carry constants. False when the matrix's digits could make a weight's sum reach
+// 2^22 (the F32 accumulation and the magic conversion would no longer be exact) or a digit would
+// not be exact in BF16; the caller then keeps the float-pair kernels.
+bool dg_build_image(const std::complex<double> M[16][16], uint32_t* bimg, int32_t (*kap)[dg::KAP]) {
+    using i128 = __int128;
+    std::memset(bimg, 0, DG_B_BYTES);
+    uint16_t* h16 = reinterpret_cast<uint16_t*>(bimg);
+    int64_t S[32];
+    int32_t rho[32][32][dg::DIGITS];  // [k][c][j]
+    for (int c = 0; c < 32; ++c) {
+        S[c] = 0;
+        for (int k = 0; k < 32; ++k) {
+            const std::complex<double> m = M[c / 2][k / 2];
+            const int o = c & 1, ii = k & 1;  // [[Re, -Im], [Im, Re]][o][ii]
+            const double val = (o == ii) ? m.real() : (o == 0 ? -m.imag() : m.imag());
+            if (!(std::fabs(val) <= 2.0)) return false;
+            int64_t R = std::llround(std::ldexp(val, 56));
+            S[c] += R;
+            for (int j = 0; j < dg::DIGITS - 1; ++j) {
+                int64_t d = R & 127;
+                if (d >= 64) d -= 128;
+                rho[k][c][j] = (int32_t)d;
+                R = (R - d) >> 7;
+            }
+            if (R > 256 || R < -256) return false;
+            rho[k][c][dg::DIGITS - 1] = (int32_t)R;
+        }
+    }
+    // exactness: every weight's sum stays below 2^22 for any register digits
+    for (int c = 0; c < 32; ++c) {
+        int64_t colsum[dg::DIGITS];
+        for (int j = 0; j < dg::DIGITS; ++j) {
+            colsum[j] = 0;
+            for (int k = 0; k < 32; ++k) colsum[j] += std::llabs(rho[k][c][j]);
+        }
+        for (int w = dg::WMIN; w <= dg::WMAX; ++w) {
+            int64_t b = 0;
+            for (int i = 0; i < dg::DIGITS; ++i) {
+                const int j = w - i;
+                if (j < 0 || j >= dg::DIGITS) continue;
+                b += (int64_t)(i == dg::DIGITS - 1 ? dg::AMAX_TOP : dg::AMAX_LOW) * colsum[j];
+            }
+            if (b >= dg::DBOUND) return false;
+        }
+    }
+    // B: chunk q = c / 16, row 16 j + c % 16, K = input real k
+    for (int c = 0; c < 32; ++c)
+        for (int j = 0; j < dg::DIGITS; ++j)
+            for (int k = 0; k < 32; ++k)
+                h16[((c / 16) * DG_B_CHUNK + dg::op_off(16 * j + c % 16, k, DG_SBO_B)) / 2] =
+                    dg_bf16(rho[k][c][j]);
+    // carry constants: K_c = 2^111 + 2^55 - (2^55 + 128 G) S_c, taken mod 2^112
+    i128 G = 0;
+    for (int i = 0; i < dg::DIGITS; ++i) G += (i128)1 << (7 * i);
+    const i128 Z = ((i128)1 << 55) + 128 * G;
+    const i128 MOD = (i128)1 << 112;
+    for (int c = 0; c < 32; ++c) {
+        i128 K = ((i128)1 << 111) + ((i128)1 << 55) - Z * (i128)S[c];
+        K %= MOD;
+        if (K < 0) K += MOD;
+        int32_t kp[16];
+        for (int p = 0; p < 16; ++p) kp[p] = (int32_t)((K >> (7 * p)) & 127);
+        const float lowc = (float)(kp[5] + 128 * kp[6] + 16384 * kp[7] - (1 << 20));
+        uint32_t lb;
+        std::memcpy(&lb, &lowc, 4);
+        kap[c][0] = (int32_t)lb;
+        kap[c][1] = (int32_t)((uint32_t)kp[8] - 2u * dg::MAGIC_BITS);
+        for (int p = 9; p <= 14; ++p) kap[c][2 + p - 9] = (int32_t)((uint32_t)kp[p] - dg::MAGIC_BITS);
+        kap[c][8] = kp[15];
+    }
+    return true;
+}
+
+bool dg_supported(const qgpu_handle* h) {
+    static const int on = [] {
+        const char* e = std::getenv("QGPU_DIGITS");  // tuning knob: 0 keeps the float-pair kernels
+        return e ? std::atoi(e) : 1;
+    }();
+    static const int min_qubits = [] {  // tuning knob: smallest register that uses them
+        const char* e = std::getenv("QGPU_DIGITS_MIN_QUBITS");
+        return std::max(11, e ? std::atoi(e) : 11);
+    }();
+    return on != 0 && h->precision == QGPU_C128 && h->mode == QGPU_MODE_FAST &&
+           (h->dim >> 4) % DG_M == 0 && h->n_qubits >= min_qubits;
+}
+
+int dg_launch_pass(qgpu_handle* h, const int bits[4], const uint32_t* bimg,
+                   const int32_t (*kap)[dg::KAP]) {
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_dg2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM);
+    QGPU_CUDA(attr);
+    DgArgs a;
+    a.nblocks = (h->dim >> 4) / DG_M;
+    for (int m = 0; m < 4; ++m) a.bits[m] = bits[m];
+    a.err = h->d_err;
+    std::memcpy(a.kap, kap, sizeof(a.kap));
+    std::memcpy(a.bimg, bimg, sizeof(a.bimg));
+    const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(a.nblocks, (uint64_t)h->sm_count));
+    k_dg2<<<(unsigned)grid, DG_THREADS, DG_SMEM, h->stream>>>((uint4*)cur_state(h), a);
+    QGPU_CHECK_LAUNCH("k_dg2");
+    h->launches++;
+    h->h2d_bytes += sizeof(a);
+    return QGPU_OK;
+}
+
+// from_layout / to_layout: 0 complex128, 1 resident float pairs
+int dg_convert(qgpu_handle* h, bool into_digits, int other_layout, int sx) {
+    const int threads = 256;
+    uint64_t blocks = (h->dim + threads - 1) / threads;
+    blocks = std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)h->sm_count * 16));
+    uint4* s = (uint4*)cur_state(h);
+    if (into_digits) {
+        if (other_layout == 0) k_dg_from<0><<<(unsigned)blocks, threads, 0, h->stream>>>(s, h->dim, sx, h->d_err);
+        else k_dg_from<1><<<(unsigned)blocks, threads, 0, h->stream>>>(s, h->dim, sx, h->d_err);
+        QGPU_CHECK_LAUNCH("k_dg_from");
+    } else {
+        if (other_layout == 0) k_dg_to<0><<<(unsigned)blocks, threads, 0, h->stream>>>(s, h->dim, sx);
+        else k_dg_to<1><<<(unsigned)blocks, threads, 0, h->stream>>>(s, h->dim, sx);
+        QGPU_CHECK_LAUNCH("k_dg_to");
+    }
+    h->launches++;
+    return QGPU_OK;
+}
+
+}  // namespace qgpu

@@ -62,6 +62,12 @@ struct qgpu_handle {
     qgpu::Scratch work;        // reductions, measurement buffers
     qgpu::Scratch work2;       // second buffer (measurement indices / adjoint vectors)
     qgpu::Scratch work3;       // adjoint: target of out-of-place index permutations
+    // An upper bound on the register's largest |amplitude| (its norm, for a normalised state):
+    // the digit passes scale their fixed point by it. Exact after set_zero (1), unknown after an
+    // upload (computed on the device when a digit pass needs it), carried through plans (Custom
+    // gates multiply it by the Frobenius norm of their effective map).
+    double norm_bound = 1.0;
+    bool norm_valid = true;
     uint64_t launches = 0;     // kernels launched on this handle (for benchmarking claims)
     uint64_t h2d_bytes = 0;    // host->device traffic: copies + kernel parameter blocks
     uint64_t d2h_bytes = 0;    // device->host copies
@@ -88,6 +94,8 @@ inline cudaError_t copy_async(qgpu_handle* h, void* dst, const void* src, size_t
     if (kind == cudaMemcpyDeviceToHost) h->d2h_bytes += n;
     return cudaMemcpyAsync(dst, src, n, kind, h->stream);
 }
+// f64 sum over the register of |a|^2 (what = 0) or of a (what = 1); synchronises.
+int reduce_state(qgpu_handle* h, int what, double2* host_out);
 // Reserves `pairs` event pairs of the handle's pool (grown on demand); *base receives the index
 // of the first one (pair i = events[2 (base + i)], events[2 (base + i) + 1]).
 int prof_events(qgpu_handle* h, size_t pairs, size_t* base);

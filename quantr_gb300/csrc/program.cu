@@ -12,12 +12,14 @@
 //    the pass's K tile bits, applies every step of the pass in registers and writes them back:
 //    one HBM round trip per pass.
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
 #include <vector>
 
+#include "digits.cuh"
 #include "internal.cuh"
 #include "plan.h"
 
@@ -1484,25 +1486,171 @@ static int launch_pair2(qgpu_handle* h, const Plan& plan, const Pass& ps, int la
     return QGPU_OK;
 }
 
+// ---- digit passes (digits.cu) ------------------------------------------------------------------
+bool dg_supported(const qgpu_handle* h);
+bool dg_build_image(const std::complex<double> M[16][16], uint32_t* bimg, int32_t (*kap)[dg::KAP]);
+int dg_launch_pass(qgpu_handle* h, const int bits[4], const uint32_t* bimg,
+                   const int32_t (*kap)[dg::KAP]);
+int dg_convert(qgpu_handle* h, bool into_digits, int other_layout, int sx);
+
+// A pair pass as a digit pass: its tile bits and the B operand / carry constants of its 16 x 16
+// matrix over the tile's physical slots.
+struct DgPass {
+    int bits[4];
+    std::vector<uint32_t> bimg;
+    std::vector<int32_t> kap;
+};
+
+static int slot_of(const int bits[4], uint64_t off) {
+    int j = 0;
+    for (int m = 0; m < 4; ++m)
+        if ((off >> bits[m]) & 1ull) j |= 1 << m;
+    return j;
+}
+
+// False when the pass cannot run as a digit pass (the matrix fails the exactness bound).
+static bool dg_pass_image(const Plan& plan, const Pass& ps, int n, DgPass* out) {
+    cd M16[16][16];
+    for (int j = 0; j < 16; ++j)
+        for (int c = 0; c < 16; ++c) M16[j][c] = 0.0;
+    if (ps.pair2 >= 0) {
+        for (int m = 0; m < 4; ++m) out->bits[m] = ps.bits[m];
+        const PairBlock* blk[2] = {&plan.pairs[ps.pair], &plan.pairs[ps.pair2]};
+        int lo[2] = {-1, -1}, hi[2] = {-1, -1};
+        for (int b = 0; b < 2; ++b)
+            for (int m = 0; m < 4; ++m) {
+                if (ps.bits[m] == blk[b]->lo) lo[b] = m;
+                if (ps.bits[m] == blk[b]->hi) hi[b] = m;
+            }
+        if (lo[0] < 0 || hi[0] < 0 || lo[1] < 0 || hi[1] < 0) return false;
+        auto lidx = [&](int b, int j) { return 2 * ((j >> hi[b]) & 1) + ((j >> lo[b]) & 1); };
+        uint64_t pre_off[16], post_off[16];
+        slot_offsets(ps.bits, ps.pre, pre_off);
+        slot_offsets(ps.bits, ps.post, post_off);
+        for (int j = 0; j < 16; ++j)        // logical output slot
+            for (int c = 0; c < 16; ++c)    // logical input slot
+                M16[slot_of(ps.bits, post_off[j])][slot_of(ps.bits, pre_off[c])] =
+                    blk[0]->m[lidx(0, j)][lidx(0, c)] * blk[1]->m[lidx(1, j)][lidx(1, c)];
+    } else if (ps.pair >= 0) {
+        // one block: its two bits and the two lowest other bits form the tile
+        const PairBlock& b = plan.pairs[ps.pair];
+        int bs[4] = {b.lo, b.hi, -1, -1}, nb = 2;
+        for (int q = 0; q < n && nb < 4; ++q)
+            if (q != b.lo && q != b.hi) bs[nb++] = q;
+        if (nb < 4) return false;
+        std::sort(bs, bs + 4);
+        for (int m = 0; m < 4; ++m) out->bits[m] = bs[m];
+        int lo = 0, hi = 0;
+        for (int m = 0; m < 4; ++m) {
+            if (bs[m] == b.lo) lo = m;
+            if (bs[m] == b.hi) hi = m;
+        }
+        const int blockmask = (1 << lo) | (1 << hi);
+        for (int j = 0; j < 16; ++j)
+            for (int c = 0; c < 16; ++c)
+                if (((j ^ c) & ~blockmask) == 0)
+                    M16[j][c] = b.m[2 * ((j >> hi) & 1) + ((j >> lo) & 1)][2 * ((c >> hi) & 1) + ((c >> lo) & 1)];
+    } else {
+        return false;
+    }
+    out->bimg.assign(4096, 0u);
+    out->kap.assign(32 * dg::KAP, 0);
+    return dg_build_image(M16, out->bimg.data(), reinterpret_cast<int32_t(*)[dg::KAP]>(out->kap.data()));
+}
+
+// Frobenius norm of a Custom gate's effective map (None inputs keep their amplitude): a bound on
+// how much it can grow the register's largest amplitude.
+static double custom_growth(const LocalGate& g) {
+    const size_t d = (size_t)1 << g.k;
+    double s = 0.0;
+    for (size_t l = 0; l < d; ++l) {
+        if (g.none[l]) {
+            s += 1.0;
+            continue;
+        }
+        for (size_t j = 0; j < d; ++j)
+            if (!g.none[j]) s += std::norm(g.M[j * d + l]);
+    }
+    return std::sqrt(s);
+}
+
+static bool is_pair_pass(const Pass& p) {
+    return p.custom < 0 && !p.xor_pass && (p.pair2 >= 0 || p.pair >= 0);
+}
+
 // Whether a float-pair plan runs on the resident layout: it saves the split and join of every
 // arithmetic pass for two extra streaming passes, so it pays once the plan carries several
-// arithmetic passes. Custom blocks read complex128 and keep the plan on the plain layout.
-// QGPU_FF_RESIDENT=0/1 forces it off/on.
-static bool plan_resident(const qgpu_handle* h, const Plan& plan) {
+// arithmetic passes (passes that run as digit passes do not count). Custom blocks read
+// complex128 and keep the plan on the plain layout. QGPU_FF_RESIDENT=0/1 forces it off/on.
+static bool plan_resident(const qgpu_handle* h, const Plan& plan, const std::vector<char>& dig) {
     if (policy_of(h) != POL_FF || !plan.customs.empty()) return false;
     static const int force = env_int("QGPU_FF_RESIDENT", -1);
     if (force >= 0) return force != 0;
     int arith = 0;
-    for (const Pass& ps : plan.passes) arith += (ps.custom < 0 && !ps.xor_pass && ps.arith);
+    for (size_t i = 0; i < plan.passes.size(); ++i) {
+        const Pass& ps = plan.passes[i];
+        arith += (!dig[i] && ps.custom < 0 && !ps.xor_pass && ps.arith);
+    }
     return arith >= 8;
 }
+
+// One launch of a plan: a pass in a given layout, or a layout conversion.
+enum LaunchKind { LK_PASS = 0, LK_FF_TO_PAIRS, LK_FF_TO_C128, LK_DG_FROM_C128, LK_DG_FROM_RES,
+                  LK_DG_TO_C128, LK_DG_TO_RES };
+constexpr int LAY_DIG = 4;  // the digit layout (digits.cuh), inside runs of pair passes
+struct LaunchItem {
+    int kind = LK_PASS;
+    int pass = -1;
+    int lay = LAY_PLAIN;
+    int sx = 0;            // digit conversions: the run's scale
+};
 
 // pre_resident: the buffer already holds the resident float-pair layout (the adjoint sweep keeps
 // its vectors that way); the passes use it as is and no layout conversion is launched.
 static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre_resident = false) {
     const int pol = policy_of(h);
-    const bool resident = pre_resident || plan_resident(h, plan);
-    const bool convert = resident && !pre_resident;
+    const size_t np = plan.passes.size();
+    // Runs of at least QGPU_DIGITS_MIN_RUN pair passes (XOR passes between them allowed: they
+    // move whole slots) run as digit passes on the tensor cores when every pass of the run passes
+    // the exactness bound; two conversion passes bracket each run.
+    std::vector<char> dig(np, 0);
+    std::vector<DgPass> dgp(np);
+    bool any_dig = false;
+    if (!pre_resident && h->active == nullptr && dg_supported(h)) {
+        static const int min_run = std::max(1, env_int("QGPU_DIGITS_MIN_RUN", 6));
+        size_t i = 0;
+        while (i < np) {
+            if (!is_pair_pass(plan.passes[i])) {
+                ++i;
+                continue;
+            }
+            size_t j = i, last = i;
+            int npair = 0;
+            while (j < np && (is_pair_pass(plan.passes[j]) || plan.passes[j].xor_pass)) {
+                if (is_pair_pass(plan.passes[j])) {
+                    last = j;
+                    ++npair;
+                }
+                ++j;
+            }
+            bool ok = npair >= min_run;
+            for (size_t k = i; ok && k <= last; ++k)
+                if (is_pair_pass(plan.passes[k])) ok = dg_pass_image(plan, plan.passes[k], h->n_qubits, &dgp[k]);
+            if (ok) {
+                for (size_t k = i; k <= last; ++k) dig[k] = 1;
+                any_dig = true;
+            }
+            i = j;
+        }
+    }
+    if (any_dig && !h->norm_valid) {  // the digit scale needs a bound on the amplitudes
+        double2 r;
+        int st = reduce_state(h, 0, &r);
+        if (st != QGPU_OK) return st;
+        h->norm_bound = std::sqrt(std::max(0.0, r.x)) * (1.0 + 1e-9);
+        h->norm_valid = true;
+    }
+    const bool resident = pre_resident || plan_resident(h, plan, dig);
     // phase tables for every TABLE step of the plan, uploaded once
     const size_t nent = plan.table_f64.size() / 2;
     const float4* tab_ff = nullptr;
@@ -1539,31 +1687,101 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
         QGPU_CUDA(copy_async(h, h->gates.ptr, host.data(), at, cudaMemcpyHostToDevice));
         QGPU_CUDA(cudaStreamSynchronize(h->stream));
     }
-    TileParams tp;
+    // The launch sequence: layouts follow the passes. Float-pair passes of a resident plan run
+    // on the resident layout; the first one that meets complex128 converts it on its loads
+    // (LAY_IN) and the plan's last non-XOR pass writes complex128 back (LAY_OUT) where it can;
+    // elsewhere a k_ff_layout pass converts. Digit runs are bracketed by k_dg_from / k_dg_to.
+    static const int fuse = env_int("QGPU_FUSE_LAYOUT", 1);  // tuning knob: 0 = separate passes
+    auto fusable = [](const Pass& p) {
+        return p.custom < 0 && !p.xor_pass && (p.pair >= 0 || (p.arith && p.nbits <= MAX_TILE_BITS));
+    };
+    int last_nonxor = (int)np - 1;
+    while (last_nonxor >= 0 && plan.passes[last_nonxor].xor_pass) --last_nonxor;
+    std::vector<LaunchItem> items;
+    items.reserve(np + 8);
+    int cur = pre_resident ? LAY_RES : LAY_PLAIN;
+    double bound = h->norm_bound;
+    int run_sx = dg::SX_UNIT;
+    bool first_arith = true;
+    for (size_t pi = 0; pi < np; ++pi) {
+        const Pass& p = plan.passes[pi];
+        LaunchItem it;
+        it.pass = (int)pi;
+        if (dig[pi]) {
+            if (cur != LAY_DIG) {
+                // scale: |x| <= bound <= 2^e, so |X| = |x| 2^sx <= 2^54
+                int e = 0;
+                if (bound > 0.0) e = (int)std::ceil(std::log2(bound));
+                run_sx = std::max(-60, std::min(100, dg::SX_UNIT - e));
+                LaunchItem cv;
+                cv.kind = cur == LAY_RES ? LK_DG_FROM_RES : LK_DG_FROM_C128;
+                cv.sx = run_sx;
+                items.push_back(cv);
+                cur = LAY_DIG;
+            }
+            it.lay = LAY_DIG;
+        } else if (p.xor_pass) {
+            it.lay = cur;  // slot moves: any layout
+        } else if (p.custom >= 0) {
+            if (cur == LAY_DIG || cur == LAY_RES) {
+                LaunchItem cv;
+                cv.kind = cur == LAY_DIG ? LK_DG_TO_C128 : LK_FF_TO_C128;
+                cv.sx = run_sx;
+                items.push_back(cv);
+                cur = LAY_PLAIN;
+            }
+            it.lay = LAY_PLAIN;
+            bound *= custom_growth(plan.customs[p.custom]);
+        } else if (resident) {
+            if (cur == LAY_DIG) {
+                LaunchItem cv;
+                cv.kind = LK_DG_TO_RES;
+                cv.sx = run_sx;
+                items.push_back(cv);
+                cur = LAY_RES;
+            }
+            const bool can_fuse = fuse && fusable(p) && !pre_resident;
+            if (cur == LAY_PLAIN && can_fuse && first_arith) {
+                it.lay = LAY_IN;
+                cur = LAY_RES;
+            } else {
+                if (cur == LAY_PLAIN) {
+                    LaunchItem cv;
+                    cv.kind = LK_FF_TO_PAIRS;
+                    items.push_back(cv);
+                    cur = LAY_RES;
+                }
+                if ((int)pi == last_nonxor && can_fuse && !first_arith) {
+                    it.lay = LAY_OUT;
+                    cur = LAY_PLAIN;
+                } else {
+                    it.lay = LAY_RES;
+                }
+            }
+            first_arith = false;
+        } else {
+            if (cur == LAY_DIG) {
+                LaunchItem cv;
+                cv.kind = LK_DG_TO_C128;
+                cv.sx = run_sx;
+                items.push_back(cv);
+                cur = LAY_PLAIN;
+            }
+            it.lay = LAY_PLAIN;
+        }
+        items.push_back(it);
+    }
+    if (!pre_resident && (cur == LAY_DIG || cur == LAY_RES)) {
+        LaunchItem cv;
+        cv.kind = cur == LAY_DIG ? LK_DG_TO_C128 : LK_FF_TO_C128;
+        cv.sx = run_sx;
+        items.push_back(cv);
+    }
+    if (!pre_resident && h->active == nullptr) h->norm_bound = bound;
+
+    const size_t nlaunch = items.size();
     std::vector<std::string> prof_names;
     std::vector<double> prof_bytes;
-    // The first and the last arithmetic pass convert the layout themselves where they can: the
-    // first pass reads complex128, and the last one writes it when only slot permutations (XOR
-    // passes, layout-agnostic) follow. Otherwise a k_ff_layout pass converts.
-    int fuse_in = -1, fuse_out = -1;
-    if (convert && !plan.passes.empty()) {
-        auto fusable = [](const Pass& p) {
-            return p.custom < 0 && !p.xor_pass && (p.pair >= 0 || (p.arith && p.nbits <= MAX_TILE_BITS));
-        };
-        static const int fuse = env_int("QGPU_FUSE_LAYOUT", 1);  // tuning knob: 0 = separate passes
-        int last = (int)plan.passes.size() - 1;
-        while (last >= 0 && plan.passes[last].xor_pass) --last;
-        if (fuse && fusable(plan.passes[0])) fuse_in = 0;
-        if (fuse && last > 0 && fusable(plan.passes[last])) fuse_out = last;
-    }
-    const bool conv_first = convert && fuse_in < 0, conv_last = convert && fuse_out < 0;
-    auto layout_of = [&](int pi) {
-        if (!resident) return (int)LAY_PLAIN;
-        if (pi == fuse_in) return (int)LAY_IN;
-        if (pi == fuse_out) return (int)LAY_OUT;
-        return (int)LAY_RES;  // (passes after fuse_out are XOR passes: any layout)
-    };
-    const size_t nlaunch = plan.passes.size() + (conv_first ? 1 : 0) + (conv_last ? 1 : 0);
     size_t ev_base = 0;
     if (h->profile) {
         int st = prof_events(h, nlaunch, &ev_base);
@@ -1572,17 +1790,19 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
     static const char* pol_name[] = {"ff", "f64", "f32"};
     QGPU_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     const double full_bytes = 2.0 * (double)h->amp_bytes * (double)h->dim;
+    TileParams tp;
     for (size_t li = 0; li < nlaunch; ++li) {
-        // launch li: [layout to pairs], passes..., [layout back]
-        const bool first_conv = conv_first && li == 0;
-        const bool last_conv = conv_last && li == nlaunch - 1;
-        const int pi = (int)li - (conv_first ? 1 : 0);
-        const Pass* ps = (first_conv || last_conv) ? nullptr : &plan.passes[pi];
-        const int play = ps ? layout_of(pi) : LAY_PLAIN;  // this pass's layout
+        const LaunchItem& it = items[li];
+        const Pass* ps = it.kind == LK_PASS ? &plan.passes[it.pass] : nullptr;
+        const int play = it.lay;
         if (h->profile) {
             QGPU_CUDA(cudaEventRecord(h->events[2 * (ev_base + li)], h->stream));
             if (!ps) {
-                prof_names.push_back("k_ff_layout");
+                prof_names.push_back(it.kind == LK_FF_TO_PAIRS || it.kind == LK_FF_TO_C128 ? "k_ff_layout"
+                                     : (it.kind == LK_DG_FROM_C128 || it.kind == LK_DG_FROM_RES) ? "k_dg_from"
+                                                                                                 : "k_dg_to");
+            } else if (play == LAY_DIG && !ps->xor_pass) {
+                prof_names.push_back("k_dg2");
             } else if (ps->pair2 >= 0) {
                 prof_names.push_back(h->precision == QGPU_C64 ? "k_pair2<f32>"
                                      : (play == LAY_RES && pair2_tc_enabled() && pair2_tc_supported(h))
@@ -1606,7 +1826,18 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
         }
         int st = QGPU_OK;
         if (!ps) {
-            st = launch_ff_layout(h, first_conv);
+            switch (it.kind) {
+                case LK_FF_TO_PAIRS: st = launch_ff_layout(h, true); break;
+                case LK_FF_TO_C128: st = launch_ff_layout(h, false); break;
+                case LK_DG_FROM_C128: st = dg_convert(h, true, 0, it.sx); break;
+                case LK_DG_FROM_RES: st = dg_convert(h, true, 1, it.sx); break;
+                case LK_DG_TO_C128: st = dg_convert(h, false, 0, it.sx); break;
+                default: st = dg_convert(h, false, 1, it.sx); break;
+            }
+        } else if (play == LAY_DIG && !ps->xor_pass) {
+            const DgPass& d = dgp[it.pass];
+            st = dg_launch_pass(h, d.bits, d.bimg.data(),
+                                reinterpret_cast<const int32_t(*)[dg::KAP]>(d.kap.data()));
         } else if (ps->pair2 >= 0) {
             st = launch_pair2(h, plan, *ps, play);
         } else if (ps->pair >= 0) {
@@ -1623,11 +1854,13 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
     }
     int st = h->profile ? prof_collect(h, prof_names, prof_bytes) : QGPU_OK;
     if (st != QGPU_OK) return st;
-    if (!sync) return QGPU_OK;  // queued; later calls on the stream are ordered after it
+    if (!sync && !any_dig) return QGPU_OK;  // queued; later calls on the stream are ordered after it
     int err = 0;
     QGPU_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
-    if (err) return fail(QGPU_ERR_TIMEOUT, "a pipelined pass gave up waiting for its bulk copies");
+    if (err == 10)
+        return fail(QGPU_ERR_INVALID, "an amplitude exceeded the bound the digit passes were scaled for");
+    if (err) return fail(QGPU_ERR_TIMEOUT, "a pipelined pass gave up waiting (code " + std::to_string(err) + ")");
     return st;
 }
 
@@ -1740,6 +1973,11 @@ extern "C" int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_o
     if (!h) return fail(QGPU_ERR_INVALID, "qgpu_apply_program: NULL handle");
     if (n_ops && !ops) return fail(QGPU_ERR_INVALID, "qgpu_apply_program: ops is NULL");
     if (n_ops == 0) return QGPU_OK;
+    // the exact and dense-block paths do not carry the amplitude bound through Custom gates
+    bool has_custom = false;
+    for (size_t g = 0; g < n_ops; ++g) has_custom = has_custom || ops[g].kind == QGPU_GATE_CUSTOM;
+    if (has_custom && ((h->precision == QGPU_C128 && h->mode == QGPU_MODE_EXACT) || h->block_qubits > 0))
+        h->norm_valid = false;
     if (h->precision == QGPU_C128 && h->mode == QGPU_MODE_EXACT) {
         std::vector<LocalGate> gates;
         gates.reserve(n_ops);

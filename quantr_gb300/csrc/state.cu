@@ -432,6 +432,8 @@ int qgpu_set_zero(qgpu_handle* h) {
         k_set_basis<float2><<<grid, threads, 0, h->stream>>>((float2*)h->state, h->dim, 0);
     QGPU_CHECK_LAUNCH("k_set_basis");
     h->launches++;
+    h->norm_bound = 1.0;
+    h->norm_valid = true;
     QGPU_CUDA(cudaStreamSynchronize(h->stream));
     return QGPU_OK;
 }
@@ -443,6 +445,7 @@ int qgpu_upload(qgpu_handle* h, const double* interleaved, size_t n_amplitudes) 
                     "qgpu_upload: the register has " + std::to_string(n_amplitudes) +
                         " amplitudes but the circuit has " + std::to_string(h->dim) +
                         " (2^" + std::to_string(h->n_qubits) + ")");
+    h->norm_valid = false;
     if (h->precision == QGPU_C128) {
         QGPU_CUDA(copy_async(h, h->state, interleaved, h->dim * 16, cudaMemcpyHostToDevice));
         QGPU_CUDA(cudaStreamSynchronize(h->stream));
