@@ -33,9 +33,10 @@ def _run(prog, reg=None, profile=False):
     return out, prof
 
 
-@pytest.mark.parametrize("n", [11, 13, 16])
+@pytest.mark.parametrize("n", [12, 14, 16])
 def test_digit_passes_run_and_match_oracle(oracle, n):
-    """The headline family: every pair pass of the brickwork runs as a digit pass."""
+    """The headline family (an even number of wires, so the brickwork's pair passes form one
+    uninterrupted run): every pair pass runs as a digit pass."""
     prog = W.brickwork_qft(n=n, layers=8, seed=5)
     ref = oracle.simulate(prog, engine=oracle.DENSE_PAR)
     out, prof = _run(prog, profile=True)
@@ -62,7 +63,7 @@ def test_digit_scale_follows_the_register(oracle, scale):
 def test_digit_runs_after_non_unitary_custom(oracle):
     """A Custom gate that grows the register (x3 on one wire) before a run of pair passes: the
     amplitude bound carried through the plan keeps the digits in range."""
-    n = 13
+    n = 14
     b = ProgramBuilder(n)
     b.add_custom(4, [], np.array([[3.0, 0.0], [0.0, 3.0]], np.complex128), np.zeros(2, np.uint8))
     rng = np.random.default_rng(8)
@@ -81,9 +82,9 @@ def test_digit_runs_after_non_unitary_custom(oracle):
 
 def test_digit_passes_with_measurement_and_norm(oracle):
     """Downstream kernels see complex128 after a digit run: norm, checksum and shots."""
-    prog = W.brickwork_qft(n=15, layers=10, seed=2)
+    prog = W.brickwork_qft(n=16, layers=10, seed=2)
     ref = oracle.simulate(prog, engine=oracle.DENSE_PAR)
-    h = nat.Handle(15)
+    h = nat.Handle(16)
     h.apply(prog.ops, prog.mats, prog.none)
     assert abs(h.norm() - 1.0) <= 1e-13
     cs = h.checksum()
