@@ -1712,7 +1712,7 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
                 // scale: |x| <= bound <= 2^e, so |X| = |x| 2^sx <= 2^54
                 int e = 0;
                 if (bound > 0.0) e = (int)std::ceil(std::log2(bound));
-                run_sx = std::max(-60, std::min(100, dg::SX_UNIT - e));
+                run_sx = std::max(-60, std::min(120, dg::SX_UNIT - e));  // 2^-120: still a normal float
                 LaunchItem cv;
                 cv.kind = cur == LAY_RES ? LK_DG_FROM_RES : LK_DG_FROM_C128;
                 cv.sx = run_sx;
