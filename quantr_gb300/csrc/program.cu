@@ -1616,7 +1616,8 @@ static int run_plan(qgpu_handle* h, const Plan& plan, bool sync = true, bool pre
     std::vector<char> dig(np, 0);
     std::vector<DgPass> dgp(np);
     bool any_dig = false;
-    if (!pre_resident && h->active == nullptr && dg_supported(h)) {
+    // (QGPU_PAIR2_TC selects the earlier tensor-core pair kernels instead)
+    if (!pre_resident && h->active == nullptr && dg_supported(h) && !pair2_tc_enabled()) {
         static const int min_run = std::max(1, env_int("QGPU_DIGITS_MIN_RUN", 6));
         size_t i = 0;
         while (i < np) {
