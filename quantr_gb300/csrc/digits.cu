@@ -15,11 +15,11 @@
 //               (M = 128 tiles, K = 16, N = 16..128) into one of three 160-column accumulators;
 //   warps 1-4   converters, one tile row each: load the tile's 16 slots (digit layout), byte-permute
 //               them into the A operand (K = 8 digits x 32 reals, BF16) of one of two buffers;
-//   warps 5-12  consumers, two groups of four warps, group g takes chunk g of every block: read the
-//               10 weights of its 16 outputs from tensor memory, run the carry chains, pack the
-//               digits and store the 8 amplitudes.
+//   warps 5-20  consumers: every job (chunk) of every block, each thread one tile row and 4 of the
+//               chunk's 16 output reals: read their 10 weights from tensor memory (all loads, then
+//               one wait), run the carry chains, pack the digits and store the 2 amplitudes.
 // Hand-offs are mbarriers: a_full[2] (128 converter arrivals), a_empty[2] (MMA commit after a
-// block's second chunk), acc_full[3] (MMA commit), acc_empty[3] (128 consumer arrivals once their
+// block's second chunk), acc_full[3] (MMA commit), acc_empty[3] (512 consumer arrivals once their
 // tensor-memory loads completed). Every wait is bounded: a wait that runs out sets the error word
 // and an abort flag that stops every role; the MMA thread drains its MMAs (bounded) before the
 // CTA frees its tensor memory.
@@ -39,7 +39,7 @@
 namespace qgpu {
 
 constexpr int DG_M = 128;                               // tiles per block (MMA rows)
-constexpr int DG_THREADS = 416;                         // 13 warps
+constexpr int DG_THREADS = 672;                         // 21 warps
 constexpr int DG_K = 256;                               // A: 8 digits x 32 reals
 constexpr uint32_t DG_SBO_A = (DG_K / 8) * 128;         // 4096: 8-row groups of A
 constexpr uint32_t DG_A_BYTES = DG_M * DG_K * 2;        // 64 KB per buffer
@@ -48,7 +48,8 @@ constexpr uint32_t DG_B_CHUNK = 128 * 32 * 2;           // 8 KB: rows 16 j + c (
 constexpr uint32_t DG_B_BYTES = 2 * DG_B_CHUNK;
 constexpr uint32_t DG_ACC_COLS = 16 * dg::NW;           // 160 columns per accumulator
 constexpr uint32_t DG_TCOLS = 512;
-constexpr size_t DG_SMEM = 2 * DG_A_BYTES + DG_B_BYTES + 1024;
+constexpr int DG_CONSUMERS = 512;                       // 16 consumer warps
+constexpr size_t DG_SMEM = 2 * DG_A_BYTES + DG_B_BYTES + 2048 + 32 * dg::KAP * 4;
 constexpr uint32_t DG_WAIT_LIMIT = 1u << 22;
 
 struct DgArgs {
@@ -81,67 +82,50 @@ __device__ __forceinline__ void dg_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Consumer side of one chunk: the 10 weights of 16 output reals (8 amplitudes) from tensor
-// memory at taddr, carry chains, packed digit slots in out[]. Arrives on `release` once every
-// tensor-memory load completed.
-template <int G>
-__device__ __forceinline__ void dg_consume(uint32_t taddr, const DgArgs& a, uint32_t release,
-                                           uint4 (&out)[8]) {
-    uint32_t x[16], y[16];
-    float low[16];
-    int32_t tp[16];   // chain values of the previous (even) position
-    int32_t tc_[16];  // chain values of the current position
-    uint32_t wd[8][4];
-    tm_ld16(taddr + 0 * 16, x);   // D_5
-    tm_wait(x);
-    tm_ld16(taddr + 1 * 16, y);   // D_6 in flight
+__device__ __forceinline__ void tm_ld4(uint32_t taddr, uint32_t (&r)[4]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
+
+// Consumer side of one job for 4 output reals (2 amplitudes: re, im, re, im) of one tile row:
+// the 10 weights of each from tensor memory at taddr (column 16 w' + output), all loads issued
+// before the one wait; arrives on `release` once they completed; then the carry chains
+// (constants kap[4][KAP] from shared memory, the same for every lane) and the packed slots.
+__device__ __forceinline__ void dg_consume4(uint32_t taddr, const int32_t* __restrict__ kap,
+                                            uint32_t release, uint4 (&out)[2]) {
+    uint32_t d[dg::NW][4];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) low[c] = __fadd_rn(__uint_as_float(x[c]), __uint_as_float((uint32_t)a.kap[16 * G + c][0]));
-    tm_wait(y);
-    tm_ld16(taddr + 2 * 16, x);   // D_7
+    for (int w = 0; w < dg::NW; ++w) tm_ld4(taddr + (uint32_t)(16 * w), d[w]);
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(d[0][0]), "+r"(d[0][1]), "+r"(d[0][2]), "+r"(d[0][3]), "+r"(d[1][0]),
+                   "+r"(d[1][1]), "+r"(d[1][2]), "+r"(d[1][3]), "+r"(d[2][0]), "+r"(d[2][1]),
+                   "+r"(d[2][2]), "+r"(d[2][3]), "+r"(d[3][0]), "+r"(d[3][1]), "+r"(d[3][2]),
+                   "+r"(d[3][3]), "+r"(d[4][0]), "+r"(d[4][1]), "+r"(d[4][2]), "+r"(d[4][3]),
+                   "+r"(d[5][0]), "+r"(d[5][1]), "+r"(d[5][2]), "+r"(d[5][3]), "+r"(d[6][0]),
+                   "+r"(d[6][1]), "+r"(d[6][2]), "+r"(d[6][3]), "+r"(d[7][0]), "+r"(d[7][1]),
+                   "+r"(d[7][2]), "+r"(d[7][3])
+                 :
+                 : "memory");
+    asm volatile("" : "+r"(d[8][0]), "+r"(d[8][1]), "+r"(d[8][2]), "+r"(d[8][3]), "+r"(d[9][0]),
+                      "+r"(d[9][1]), "+r"(d[9][2]), "+r"(d[9][3])::"memory");
+    tc::fence_before_sync();
+    dg_arrive(release);
+    int32_t t[4][8];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) low[c] = __fmaf_rn(__uint_as_float(y[c]), 128.0f, low[c]);
-    tm_wait(x);
-    tm_ld16(taddr + 3 * 16, y);   // D_8
+    for (int c = 0; c < 4; ++c) {
+        float f[dg::NW];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-        low[c] = __fmaf_rn(__uint_as_float(x[c]), 16384.0f, low[c]);
-        low[c] = __fmaf_rn(low[c], 1.0f / 2097152.0f, dg::MAGIC_F);
+        for (int w = 0; w < dg::NW; ++w) f[w] = __uint_as_float(d[w][c]);
+        dg::chain(f, kap + dg::KAP * c, t[c]);
     }
-    tm_wait(y);
-    tm_ld16(taddr + 4 * 16, x);   // D_9
 #pragma unroll
-    for (int c = 0; c < 16; ++c) tp[c] = dg::chain_first(__uint_as_float(y[c]), low[c], a.kap[16 * G + c][1]);
-    // positions 9..14: odd positions complete a word with the previous even one
+    for (int u = 0; u < 2; ++u) {
+        uint32_t w4[4];
 #pragma unroll
-    for (int p = 9; p <= 14; ++p) {
-        uint32_t(&cur)[16] = (p & 1) ? x : y;
-        uint32_t(&nxt)[16] = (p & 1) ? y : x;
-        tm_wait(cur);
-        if (p < 14) {
-            tm_ld16(taddr + (uint32_t)(p + 1 - dg::WMIN) * 16, nxt);
-        } else {  // every load of this accumulator completed: hand it back to the MMAs
-            tc::fence_before_sync();
-            dg_arrive(release);
-        }
-        if (p & 1) {
-#pragma unroll
-            for (int c = 0; c < 16; ++c) tc_[c] = dg::chain_next(__uint_as_float(cur[c]), tp[c], a.kap[16 * G + c][2 + p - 9]);
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                wd[u][(p - 9) / 2] = dg::out_word(tp[2 * u], tp[2 * u + 1], tc_[2 * u], tc_[2 * u + 1]);
-        } else {
-#pragma unroll
-            for (int c = 0; c < 16; ++c) tp[c] = dg::chain_next(__uint_as_float(cur[c]), tc_[c], a.kap[16 * G + c][2 + p - 9]);
-        }
-    }
-    // position 15 (no weight of its own) pairs with position 14 (in tp)
-#pragma unroll
-    for (int c = 0; c < 16; ++c) tc_[c] = a.kap[16 * G + c][8] + (tp[c] >> 7);
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-        wd[u][3] = dg::out_word(tp[2 * u], tp[2 * u + 1], tc_[2 * u], tc_[2 * u + 1]);
-        out[u] = make_uint4(wd[u][0], wd[u][1], wd[u][2], wd[u][3]);
+        for (int m = 0; m < 4; ++m)
+            w4[m] = dg::out_word(t[2 * u][2 * m], t[2 * u + 1][2 * m], t[2 * u][2 * m + 1], t[2 * u + 1][2 * m + 1]);
+        out[u] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
     }
 }
 
@@ -154,6 +138,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
     uint64_t* bars = reinterpret_cast<uint64_t*>(tail);  // a_full[2] a_empty[2] acc_full[3] acc_empty[3] drain
     uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 128);
     int* abort_flag = reinterpret_cast<int*>(tail + 132);
+    int32_t* skap = reinterpret_cast<int32_t*>(tail + 2048);  // carry constants [32][KAP]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t b_afull = smem_u32(bars), b_aempty = smem_u32(bars + 2),
                    b_accfull = smem_u32(bars + 4), b_accempty = smem_u32(bars + 7),
@@ -161,6 +146,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
 
     for (int i = tid; i < (int)(DG_B_BYTES / 4); i += DG_THREADS)
         reinterpret_cast<uint32_t*>(sB)[i] = a.bimg[i];
+    for (int i = tid; i < 32 * dg::KAP; i += DG_THREADS) skap[i] = (&a.kap[0][0])[i];
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) {
             mbar_init(b_afull + 8 * s, DG_M);
@@ -168,7 +154,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
         }
         for (int s = 0; s < 3; ++s) {
             mbar_init(b_accfull + 8 * s, 1);
-            mbar_init(b_accempty + 8 * s, DG_M);
+            mbar_init(b_accempty + 8 * s, DG_CONSUMERS);
         }
         mbar_init(b_drain, 1);
         *abort_flag = 0;
@@ -281,26 +267,32 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
             }
         }
     } else {  // ------------------------------------------------------------------- consumers
-        const int g = (warp - 5) >> 2;
+        // warp 5 + 4 sub + k: tensor-memory lanes 32 (warp % 4) (the tile rows it may read) and
+        // output reals 4 sub .. 4 sub + 3 of every job's chunk (amplitudes 2 sub, 2 sub + 1)
+        const int sub = (warp - 5) >> 2;
         const int quad = warp & 3;
         const int r = 32 * quad + lane;
         for (uint64_t it = 0; it < nmine; ++it) {
-            const uint64_t t = 2 * it + (uint64_t)g;
-            const int ai = (int)(t % 3);
-            if (!mbar_wait_bounded(b_accfull + 8 * ai, (uint32_t)((t / 3) & 1), DG_WAIT_LIMIT)) {
-                fail_now(9);
-                break;
-            }
-            if (aborted()) break;
-            tc::fence_after_sync();
-            const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + DG_ACC_COLS * (uint32_t)ai;
-            uint4 out[8];
-            if (g == 0) dg_consume<0>(taddr, a, b_accempty + 8 * ai, out);
-            else dg_consume<1>(taddr, a, b_accempty + 8 * ai, out);
             const uint64_t base = tile_base(blockIdx.x + it * gridDim.x, r);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) st[base | slot_off(8 * g + u)] = out[u];
+#pragma unroll 1
+            for (int q = 0; q < 2; ++q) {
+                const uint64_t t = 2 * it + (uint64_t)q;
+                const int ai = (int)(t % 3);
+                if (!mbar_wait_bounded(b_accfull + 8 * ai, (uint32_t)((t / 3) & 1), DG_WAIT_LIMIT)) {
+                    fail_now(9);
+                    goto consumers_done;
+                }
+                if (aborted()) goto consumers_done;
+                tc::fence_after_sync();
+                const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + DG_ACC_COLS * (uint32_t)ai +
+                                       (uint32_t)(4 * sub);
+                uint4 out[2];
+                dg_consume4(taddr, skap + dg::KAP * (16 * q + 4 * sub), b_accempty + 8 * ai, out);
+                st[base | slot_off(8 * q + 2 * sub)] = out[0];
+                st[base | slot_off(8 * q + 2 * sub + 1)] = out[1];
+            }
         }
+    consumers_done:;
     }
     tc::fence_before_sync();
     __syncthreads();
