@@ -11,10 +11,12 @@
 // amplitude) and run the carry chains (about 70 operations per amplitude).
 //
 // k_dg2: one CTA per SM, persistent over blocks of 128 tiles, warp-specialised:
-//   warp 0      lane 0 issues the MMAs: per block two chunks of 16 output reals, each 20 MMAs
-//               (M = 128 tiles, K = 16, N = 16..128) into one of three 160-column accumulators;
-//   warps 1-4   converters, one tile row each: load the tile's 16 slots (digit layout), byte-permute
-//               them into the A operand (K = 8 digits x 32 reals, BF16) of one of two buffers;
+//   warp 0      lane 0 issues the MMAs: per block two chunks of 16 output reals, each one seed MMA
+//               (every accumulator column := 1.5 * 2^23) and 20 MMAs (M = 128 tiles, K = 16,
+//               N = 16..128) into one of three 160-column accumulators;
+//   warps 1-4   converters, one tile row each: copy the tile's 16 slots (digit layout) to shared
+//               memory with cp.async two blocks ahead, byte-permute them into the A operand
+//               (K = 8 digits x 32 reals, BF16) of one of two buffers;
 //   warps 5-20  consumers: every job (chunk) of every block, each thread one tile row and 4 of the
 //               chunk's 16 output reals: read their 10 weights from tensor memory (all loads, then
 //               one wait), run the carry chains, pack the digits and store the 2 amplitudes.
@@ -49,7 +51,12 @@ constexpr uint32_t DG_B_BYTES = 2 * DG_B_CHUNK;
 constexpr uint32_t DG_ACC_COLS = 16 * dg::NW;           // 160 columns per accumulator
 constexpr uint32_t DG_TCOLS = 512;
 constexpr int DG_CONSUMERS = 512;                       // 16 consumer warps
-constexpr size_t DG_SMEM = 2 * DG_A_BYTES + DG_B_BYTES + 2048 + 32 * dg::KAP * 4;
+constexpr uint32_t DG_STAGE_BYTES = DG_M * 16 * 16;    // 32 KB: one block's slots
+constexpr uint32_t DG_SBO_SEED = (16 / 8) * 128;      // 256: 8-row groups of the K = 16 seed operands
+constexpr uint32_t DG_ONE_BYTES = DG_M * 16 * 2;        // 4 KB: A of the seed MMA (a ones column)
+constexpr uint32_t DG_MAGIC_BYTES = DG_ACC_COLS * 16 * 2;  // 5 KB: B of the seed MMA (MAGIC_F row)
+constexpr size_t DG_SMEM = 2 * DG_A_BYTES + DG_B_BYTES + 2 * DG_STAGE_BYTES + DG_ONE_BYTES +
+                           DG_MAGIC_BYTES + 2048 + 32 * dg::KAP * 4;
 constexpr uint32_t DG_WAIT_LIMIT = 1u << 22;
 
 struct DgArgs {
@@ -90,8 +97,9 @@ __device__ __forceinline__ void tm_ld4(uint32_t taddr, uint32_t (&r)[4]) {
 
 // Consumer side of one job for 4 output reals (2 amplitudes: re, im, re, im) of one tile row:
 // the 10 weights of each from tensor memory at taddr (column 16 w' + output), all loads issued
-// before the one wait; arrives on `release` once they completed; then the carry chains
-// (constants kap[4][KAP] from shared memory, the same for every lane) and the packed slots.
+// before the one wait; arrives on `release` once they completed; then the carry chains (kap:
+// the outputs' constants in shared memory, [KAP][32] from the first of them, the same for every
+// lane) and the packed slots.
 __device__ __forceinline__ void dg_consume4(uint32_t taddr, const int32_t* __restrict__ kap,
                                             uint32_t release, uint4 (&out)[2]) {
     uint32_t d[dg::NW][4];
@@ -111,34 +119,57 @@ __device__ __forceinline__ void dg_consume4(uint32_t taddr, const int32_t* __res
                       "+r"(d[9][1]), "+r"(d[9][2]), "+r"(d[9][3])::"memory");
     tc::fence_before_sync();
     dg_arrive(release);
-    int32_t t[4][8];
+    // the four chains run position by position; kap is [KAP][32] in shared memory, so one 16-byte
+    // load gives constant i of the thread's four outputs
+    const int4* k4 = reinterpret_cast<const int4*>(kap);
+    auto kc = [](const int4& v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; };
+    float low[4];
+    int32_t tp[4], tq[4];
+    uint32_t w4[2][4];
+    {
+        const int4 k0 = k4[0];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        float f[dg::NW];
+        for (int c = 0; c < 4; ++c)
+            low[c] = dg::chain_low(__uint_as_float(d[0][c]), __uint_as_float(d[1][c]), __uint_as_float(d[2][c]), kc(k0, c));
+        const int4 k1 = k4[8];
 #pragma unroll
-        for (int w = 0; w < dg::NW; ++w) f[w] = __uint_as_float(d[w][c]);
-        dg::chain(f, kap + dg::KAP * c, t[c]);
+        for (int c = 0; c < 4; ++c) tp[c] = dg::chain_first(__uint_as_float(d[3][c]), low[c], kc(k1, c));
     }
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        uint32_t w4[4];
+    for (int p = 9; p <= 15; p += 2) {  // positions p (odd) and p + 1 (even, or none after 15)
+        const int4 kp = k4[8 * (2 + p - 9)];
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-            w4[m] = dg::out_word(t[2 * u][2 * m], t[2 * u + 1][2 * m], t[2 * u][2 * m + 1], t[2 * u + 1][2 * m + 1]);
-        out[u] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+        for (int c = 0; c < 4; ++c)
+            tq[c] = p < 15 ? dg::chain_next(__uint_as_float(d[p - dg::WMIN][c]), tp[c], kc(kp, c))
+                           : kc(kp, c) + (tp[c] >> 7);
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+            w4[u][(p - 9) / 2] = dg::out_word(tp[2 * u], tp[2 * u + 1], tq[2 * u], tq[2 * u + 1]);
+        if (p < 15) {
+            const int4 kn = k4[8 * (2 + p + 1 - 9)];
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                tp[c] = p + 1 < 15 ? dg::chain_next(__uint_as_float(d[p + 1 - dg::WMIN][c]), tq[c], kc(kn, c))
+                                   : kc(kn, c) + (tq[c] >> 7);
+        }
     }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) out[u] = make_uint4(w4[u][0], w4[u][1], w4[u][2], w4[u][3]);
 }
 
-__global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
+__global__ void __maxnreg__(96) k_dg2(uint4* __restrict__ st,
                                                        const __grid_constant__ DgArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* sA = sm;
     uint8_t* sB = sm + 2 * DG_A_BYTES;
-    uint8_t* tail = sB + DG_B_BYTES;
+    uint8_t* sStage = sB + DG_B_BYTES;  // 2 x 32 KB: converters' staging of the state
+    uint8_t* sOne = sStage + 2 * DG_STAGE_BYTES;
+    uint8_t* sMagic = sOne + DG_ONE_BYTES;
+    uint8_t* tail = sMagic + DG_MAGIC_BYTES;
     uint64_t* bars = reinterpret_cast<uint64_t*>(tail);  // a_full[2] a_empty[2] acc_full[3] acc_empty[3] drain
     uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 128);
     int* abort_flag = reinterpret_cast<int*>(tail + 132);
-    int32_t* skap = reinterpret_cast<int32_t*>(tail + 2048);  // carry constants [32][KAP]
+    int32_t* skap = reinterpret_cast<int32_t*>(tail + 2048);  // carry constants [KAP][32]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t b_afull = smem_u32(bars), b_aempty = smem_u32(bars + 2),
                    b_accfull = smem_u32(bars + 4), b_accempty = smem_u32(bars + 7),
@@ -146,7 +177,15 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
 
     for (int i = tid; i < (int)(DG_B_BYTES / 4); i += DG_THREADS)
         reinterpret_cast<uint32_t*>(sB)[i] = a.bimg[i];
-    for (int i = tid; i < 32 * dg::KAP; i += DG_THREADS) skap[i] = (&a.kap[0][0])[i];
+    for (int i = tid; i < 32 * dg::KAP; i += DG_THREADS) skap[i] = a.kap[i % 32][i / 32];
+    // seed operands: A = e_0 in every row (BF16 1.0 at k = 0), B = MAGIC_F at k = 0 in every row
+    for (int i = tid; i < (int)((DG_ONE_BYTES + DG_MAGIC_BYTES) / 2); i += DG_THREADS) {
+        const bool one = i < (int)(DG_ONE_BYTES / 2);
+        const int e = one ? i : i - (int)(DG_ONE_BYTES / 2);
+        const int row = e / 16, k = e % 16;
+        const uint16_t v = k != 0 ? 0 : (one ? 0x3F80 : 0x4B40);  // BF16 1.0 / 1.5 * 2^23
+        *reinterpret_cast<uint16_t*>((one ? sOne : sMagic) + dg::op_off(row, k, DG_SBO_SEED)) = v;
+    }
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) {
             mbar_init(b_afull + 8 * s, DG_M);
@@ -187,6 +226,10 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
     if (warp == 0) {  // ------------------------------------------------------------ MMA issue
         if (lane == 0) {
             bool issued = false;
+            const uint64_t a_desc0 = tc::smem_desc(smem_u32(sA), 128, DG_SBO_A);
+            const uint64_t b_desc0 = tc::smem_desc(smem_u32(sB), 128, DG_SBO_B);
+            const uint64_t one_desc = tc::smem_desc(smem_u32(sOne), 128, DG_SBO_SEED);
+            const uint64_t magic_desc = tc::smem_desc(smem_u32(sMagic), 128, DG_SBO_SEED);
             for (uint64_t t = 0; t < 2 * nmine; ++t) {
                 const uint64_t it = t >> 1;
                 const int q = (int)(t & 1), s = (int)(it & 1), ai = (int)(t % 3);
@@ -201,21 +244,20 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
                 }
                 if (aborted()) break;
                 tc::fence_after_sync();
-                const uint32_t sa = smem_u32(sA + (uint32_t)s * DG_A_BYTES);
-                const uint32_t sb = smem_u32(sB + (uint32_t)q * DG_B_CHUNK);
                 const uint32_t acc = tmem + DG_ACC_COLS * (uint32_t)ai;
+                // descriptors: base + the operand's byte offset / 16 (the start-address field)
+                const uint64_t ad0 = a_desc0 + (uint64_t)((s * DG_A_BYTES) >> 4);
+                const uint64_t bd0 = b_desc0 + (uint64_t)((q * DG_B_CHUNK) >> 4);
+                tc::mma_bf16(acc, one_desc, magic_desc, tc::idesc_bf16(DG_M, (int)DG_ACC_COLS), 0u);
 #pragma unroll
                 for (int k = 0; k < dg::NSTEPS; ++k) {
                     const dg::MmaStep ms = dg::mma_step(k);
                     const uint32_t idesc = tc::idesc_bf16(DG_M, 16 * (ms.jend - ms.jmin));
 #pragma unroll
-                    for (int kk = 0; kk < 2; ++kk) {
-                        const uint64_t ad = tc::smem_desc(sa + (uint32_t)(4 * ms.i + 2 * kk) * 128, 128, DG_SBO_A);
-                        const uint64_t bd =
-                            tc::smem_desc(sb + (uint32_t)ms.jmin * 1024 + (uint32_t)kk * 256, 128, DG_SBO_B);
-                        tc::mma_bf16(acc + (uint32_t)(16 * (ms.i + ms.jmin - dg::WMIN)), ad, bd, idesc,
-                                     (ms.init && kk == 0) ? 0u : 1u);
-                    }
+                    for (int kk = 0; kk < 2; ++kk)
+                        tc::mma_bf16(acc + (uint32_t)(16 * (ms.i + ms.jmin - dg::WMIN)),
+                                     ad0 + (uint64_t)(((4 * ms.i + 2 * kk) * 128) >> 4),
+                                     bd0 + (uint64_t)((ms.jmin * 1024 + kk * 256) >> 4), idesc, 1u);
                 }
                 issued = true;
                 tc::commit(b_accfull + 8 * ai);
@@ -228,30 +270,44 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
         }
         __syncwarp();
     } else if (warp <= 4) {  // ------------------------------------------------------ converters
+        // Each thread copies its tile row's 16 slots global -> shared with cp.async into one of two
+        // stages (slot j of row r at stage[j * 128 + r]: conflict-free for the warp), two blocks
+        // ahead of the block it converts, so no registers are held while the loads fly.
         const int r = tid - 32;
-        uint4 v[16];
-        if (nmine > 0) {
-            const uint64_t b0 = tile_base(blockIdx.x, r);
+        auto issue = [&](uint64_t it) {
+            const uint64_t b0 = tile_base(blockIdx.x + it * gridDim.x, r);
+            uint8_t* dst = sStage + (uint32_t)(it & 1) * DG_STAGE_BYTES;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] = st[b0 | slot_off(j)];
-        }
+            for (int j = 0; j < 16; ++j)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst + (j * DG_M + r) * 16)),
+                             "l"(st + (b0 | slot_off(j)))
+                             : "memory");
+        };
+        if (nmine > 0) issue(0);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        if (nmine > 1) issue(1);
+        asm volatile("cp.async.commit_group;" ::: "memory");
         for (uint64_t it = 0; it < nmine; ++it) {
             const int s = (int)(it & 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");  // block it's group is complete
             if (it >= 2 && !mbar_wait_bounded(b_aempty + 8 * s, (uint32_t)(((it >> 1) - 1) & 1), DG_WAIT_LIMIT)) {
                 fail_now(8);
                 break;
             }
             if (aborted()) break;
+            const uint8_t* src = sStage + (uint32_t)s * DG_STAGE_BYTES;
             uint8_t* A = sA + (uint32_t)s * DG_A_BYTES;
 #pragma unroll
-            for (int i = 0; i < dg::DIGITS; ++i) {
+            for (int g = 0; g < 4; ++g) {  // slots 4g..4g+3: one 16-byte row of each digit's core matrix
+                uint4 v[4];
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
+                for (int q = 0; q < 4; ++q) v[q] = *reinterpret_cast<const uint4*>(src + ((4 * g + q) * DG_M + r) * 16);
+#pragma unroll
+                for (int i = 0; i < dg::DIGITS; ++i) {
                     uint32_t w[4];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        const uint4 s4 = v[4 * g + q];
-                        const uint32_t sw = (i >> 1) == 0 ? s4.x : (i >> 1) == 1 ? s4.y : (i >> 1) == 2 ? s4.z : s4.w;
+                        const uint32_t sw = (i >> 1) == 0 ? v[q].x : (i >> 1) == 1 ? v[q].y : (i >> 1) == 2 ? v[q].z : v[q].w;
                         w[q] = dg::a_word(sw, i & 1);
                     }
                     *reinterpret_cast<uint4*>(A + dg::op_off(r, 32 * i + 8 * g, DG_SBO_A)) =
@@ -260,12 +316,10 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
             }
             fence_proxy_async_shared();  // the generic-proxy writes of A visible to the MMAs
             dg_arrive(b_afull + 8 * s);
-            if (it + 1 < nmine) {  // the next block's loads fly while this one waits
-                const uint64_t bn = tile_base(blockIdx.x + (it + 1) * gridDim.x, r);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = st[bn | slot_off(j)];
-            }
+            if (it + 2 < nmine) issue(it + 2);  // refills the stage just read
+            asm volatile("cp.async.commit_group;" ::: "memory");
         }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");  // nothing in flight at exit
     } else {  // ------------------------------------------------------------------- consumers
         // warp 5 + 4 sub + k: tensor-memory lanes 32 (warp % 4) (the tile rows it may read) and
         // output reals 4 sub .. 4 sub + 3 of every job's chunk (amplitudes 2 sub, 2 sub + 1)
@@ -287,7 +341,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
                 const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + DG_ACC_COLS * (uint32_t)ai +
                                        (uint32_t)(4 * sub);
                 uint4 out[2];
-                dg_consume4(taddr, skap + dg::KAP * (16 * q + 4 * sub), b_accempty + 8 * ai, out);
+                dg_consume4(taddr, skap + 16 * q + 4 * sub, b_accempty + 8 * ai, out);
                 st[base | slot_off(8 * q + 2 * sub)] = out[0];
                 st[base | slot_off(8 * q + 2 * sub + 1)] = out[1];
             }
@@ -476,7 +530,8 @@ bool dg_build_image(const std::complex<double> M[16][16], uint32_t* bimg, int32_
         if (K < 0) K += MOD;
         int32_t kp[16];
         for (int p = 0; p < 16; ++p) kp[p] = (int32_t)((K >> (7 * p)) & 127);
-        const float lowc = (float)(kp[5] + 128 * kp[6] + 16384 * kp[7] - (1 << 20));
+        const float lowc = (float)((double)(kp[5] + 128 * kp[6] + 16384 * kp[7] - (1 << 20)) -
+                                   16513.0 * (double)dg::MAGIC_F);
         uint32_t lb;
         std::memcpy(&lb, &lowc, 4);
         kap[c][0] = (int32_t)lb;

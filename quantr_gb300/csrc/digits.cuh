@@ -122,11 +122,13 @@ __host__ __device__ __forceinline__ uint32_t out_word(int32_t pr, int32_t pi, in
     return ((x & 0x0000FFFFu) | (y & 0xFFFF0000u)) & 0x7F7F7F7Fu;
 }
 
-// Carry chain of one output real. d[0..9] = D_5..D_14 (integer-valued floats below 2^22),
-// kap[] its constants: kap[0] = bits of (float)(k5 + 128 k6 + 16384 k7 - 2^20), kap[1] =
-// k8 - 2 MAGIC_BITS, kap[2 + p - 9] = k_p - MAGIC_BITS for p = 9..14, kap[8] = k15 (k_p: the base-128
-// digits of K_c mod 2^112). t[0..7] receive the chain values of positions 8..15; their low 7
-// bits are the output digits. The kernels run the same operations spread over their loads.
+// Carry chain of one output real. The accumulators start at MAGIC_F (one MMA of a ones column
+// against a row of MAGIC_F seeds them), so d[0..9] = MAGIC_F + D_5 .. MAGIC_F + D_14 exactly
+// (|D_w| < 2^22) and their bits are MAGIC_BITS + D_w. kap[] holds the constants: kap[0] = bits
+// of (float)(k5 + 128 k6 + 16384 k7 - 2^20 - 16513 MAGIC_F) (the low part, taken in float),
+// kap[1] = k8 - 2 MAGIC_BITS, kap[2 + p - 9] = k_p - MAGIC_BITS for p = 9..14, kap[8] = k15 (k_p:
+// the base-128 digits of K_c mod 2^112). t[0..7] receive the chain values of positions 8..15;
+// their low 7 bits are the output digits. The kernels run the same operations.
 __host__ __device__ __forceinline__ float chain_low(float d5, float d6, float d7, int32_t kap0) {
     float lo = add_rn(d5, u2f((uint32_t)kap0));
     lo = fma_rn(d6, 128.0f, lo);
@@ -134,10 +136,10 @@ __host__ __device__ __forceinline__ float chain_low(float d5, float d6, float d7
     return fma_rn(lo, 1.0f / 2097152.0f, MAGIC_F);  // its bits: MAGIC + floor(low / 2^21) (+-1)
 }
 __host__ __device__ __forceinline__ int32_t chain_first(float d8, float low, int32_t kap1) {
-    return (int32_t)(f2u(add_rn(d8, MAGIC_F)) + f2u(low) + (uint32_t)kap1);
+    return (int32_t)(f2u(d8) + f2u(low) + (uint32_t)kap1);
 }
 __host__ __device__ __forceinline__ int32_t chain_next(float dp, int32_t prev, int32_t kapp) {
-    return (int32_t)(f2u(add_rn(dp, MAGIC_F)) + (uint32_t)kapp + (uint32_t)(prev >> 7));
+    return (int32_t)(f2u(dp) + (uint32_t)kapp + (uint32_t)(prev >> 7));
 }
 __host__ __device__ __forceinline__ void chain(const float d[NW], const int32_t kap[KAP], int32_t t[8]) {
     const float low = chain_low(d[0], d[1], d[2], kap[0]);
@@ -147,8 +149,9 @@ __host__ __device__ __forceinline__ void chain(const float d[NW], const int32_t 
 }
 
 // The MMAs of one chunk (16 output reals): digit i of A times matrix digits j in [jmin, jend)
-// into the weights i + j, the first MMA touching a weight initialising it. Every pair with
-// i + j >= WMIN appears once (49 pairs).
+// into the weights i + j, all accumulating onto the MAGIC_F seed. Every pair with i + j >= WMIN
+// appears once (49 pairs). (`init` marks the first step touching each weight; unused since the
+// seed MMA initialises every weight.)
 struct MmaStep {
     int i, jmin, jend, init;
 };

@@ -102,7 +102,7 @@ static double run_tile(const cdd M[16][16], const uint32_t* bimg, const int32_t 
         for (int part = 0; part < 2; ++part) {
             const int c = 2 * u + part;
             float d[dg::NW];
-            for (int w = 0; w < dg::NW; ++w) d[w] = (float)D[c][w];
+            for (int w = 0; w < dg::NW; ++w) d[w] = (float)(D[c][w] + (int64_t)dg::MAGIC_F);  // seeded accumulator
             dg::chain(d, kap[c], t[part]);
         }
         uint32_t w4[4];
