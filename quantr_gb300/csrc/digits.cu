@@ -41,7 +41,7 @@
 namespace qgpu {
 
 constexpr int DG_M = 128;                               // tiles per block (MMA rows)
-constexpr int DG_THREADS = 672;                         // 21 warps
+constexpr int DG_THREADS = 672;                         // 21 warps: 6 on some SM sub-partition, so 80 registers
 constexpr int DG_K = 256;                               // A: 8 digits x 32 reals
 constexpr uint32_t DG_SBO_A = (DG_K / 8) * 128;         // 4096: 8-row groups of A
 constexpr uint32_t DG_A_BYTES = DG_M * DG_K * 2;        // 64 KB per buffer
@@ -157,7 +157,7 @@ __device__ __forceinline__ void dg_consume4(uint32_t taddr, const int32_t* __res
     for (int u = 0; u < 2; ++u) out[u] = make_uint4(w4[u][0], w4[u][1], w4[u][2], w4[u][3]);
 }
 
-__global__ void __maxnreg__(96) k_dg2(uint4* __restrict__ st,
+__global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
                                                        const __grid_constant__ DgArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* sA = sm;
