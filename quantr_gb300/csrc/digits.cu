@@ -11,20 +11,22 @@
 // amplitude) and run the carry chains (about 70 operations per amplitude).
 //
 // k_dg2: one CTA per SM, persistent over blocks of 128 tiles, warp-specialised:
-//   warp 0      lane 0 issues the MMAs: per block two chunks of 16 output reals, each one seed MMA
-//               (every accumulator column := 1.5 * 2^23) and 20 MMAs (M = 128 tiles, K = 16,
-//               N = 16..128) into one of three 160-column accumulators;
+//   warp 0      lane 0 issues the MMAs of a block into the one 320-column accumulator (10 weights
+//               x 32 output reals): two seed MMAs (every column := 1.5 * 2^23), then for each digit
+//               i of A one MMA per K half over the matrix digits j it pairs with (M = 128 tiles,
+//               K = 16, N = 32 per digit, up to 256), so every A slice is read once per block;
 //   warps 1-4   converters, one tile row each: copy the tile's 16 slots (digit layout) to shared
 //               memory with cp.async two blocks ahead, byte-permute them into the A operand
 //               (K = 8 digits x 32 reals, BF16) of one of two buffers;
-//   warps 5-20  consumers: every job (chunk) of every block, each thread one tile row and 4 of the
-//               chunk's 16 output reals: read their 10 weights from tensor memory (all loads, then
-//               one wait), run the carry chains, pack the digits and store the 2 amplitudes.
-// Hand-offs are mbarriers: a_full[2] (128 converter arrivals), a_empty[2] (MMA commit after a
-// block's second chunk), acc_full[3] (MMA commit), acc_empty[3] (512 consumer arrivals once their
-// tensor-memory loads completed). Every wait is bounded: a wait that runs out sets the error word
-// and an abort flag that stops every role; the MMA thread drains its MMAs (bounded) before the
-// CTA frees its tensor memory.
+//   warps 5-20  consumers: every block, each thread one tile row and output reals 4 s .. 4 s + 3 and
+//               16 + 4 s .. 16 + 4 s + 3: read their 10 weights from tensor memory (all loads, then
+//               one wait), run the carry chains, pack the digits and store the 4 amplitudes.
+// Hand-offs are mbarriers: a_full[2] (128 converter arrivals), a_empty[2] (MMA commit after the
+// block), acc_full (MMA commit), acc_empty (512 consumer arrivals once their tensor-memory loads
+// completed). Every wait is bounded: a wait that runs out sets the error word and an abort flag
+// that stops every role; the MMA thread drains its MMAs (bounded) before the CTA frees its
+// tensor memory. Shared memory per block read by the tensor cores: A 80 KB, B 100 KB (the chunked
+// form, which re-read A per 16 outputs, was bound by shared-memory bandwidth).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -46,15 +48,15 @@ constexpr int DG_K = 256;                               // A: 8 digits x 32 real
 constexpr uint32_t DG_SBO_A = (DG_K / 8) * 128;         // 4096: 8-row groups of A
 constexpr uint32_t DG_A_BYTES = DG_M * DG_K * 2;        // 64 KB per buffer
 constexpr uint32_t DG_SBO_B = (32 / 8) * 128;           // 512: 8-row groups of B (K = 32)
-constexpr uint32_t DG_B_CHUNK = 128 * 32 * 2;           // 8 KB: rows 16 j + c (8 digits x 16 outputs)
-constexpr uint32_t DG_B_BYTES = 2 * DG_B_CHUNK;
-constexpr uint32_t DG_ACC_COLS = 16 * dg::NW;           // 160 columns per accumulator
+constexpr uint32_t DG_B_BYTES = 256 * 32 * 2;           // 16 KB: rows 32 j + c (8 digits x 32 outputs)
+constexpr uint32_t DG_ACC_COLS = 32 * dg::NW;           // 320 columns: weight-major, 32 outputs each
 constexpr uint32_t DG_TCOLS = 512;
 constexpr int DG_CONSUMERS = 512;                       // 16 consumer warps
 constexpr uint32_t DG_STAGE_BYTES = DG_M * 16 * 16;    // 32 KB: one block's slots
 constexpr uint32_t DG_SBO_SEED = (16 / 8) * 128;      // 256: 8-row groups of the K = 16 seed operands
 constexpr uint32_t DG_ONE_BYTES = DG_M * 16 * 2;        // 4 KB: A of the seed MMA (a ones column)
-constexpr uint32_t DG_MAGIC_BYTES = DG_ACC_COLS * 16 * 2;  // 5 KB: B of the seed MMA (MAGIC_F row)
+constexpr uint32_t DG_SEED_N = DG_ACC_COLS / 2;         // two seed MMAs of N = 160
+constexpr uint32_t DG_MAGIC_BYTES = DG_SEED_N * 16 * 2;  // 5 KB: B of the seed MMA (MAGIC_F row)
 constexpr size_t DG_SMEM = 2 * DG_A_BYTES + DG_B_BYTES + 2 * DG_STAGE_BYTES + DG_ONE_BYTES +
                            DG_MAGIC_BYTES + 2048 + 32 * dg::KAP * 4;
 constexpr uint32_t DG_WAIT_LIMIT = 1u << 22;
@@ -96,15 +98,15 @@ __device__ __forceinline__ void tm_ld4(uint32_t taddr, uint32_t (&r)[4]) {
 }
 
 // Consumer side of one job for 4 output reals (2 amplitudes: re, im, re, im) of one tile row:
-// the 10 weights of each from tensor memory at taddr (column 16 w' + output), all loads issued
-// before the one wait; arrives on `release` once they completed; then the carry chains (kap:
+// the 10 weights of each from tensor memory at taddr (column 32 w' + output), all loads issued
+// before the one wait; arrives on `release` (when not 0) once they completed; then the carry chains (kap:
 // the outputs' constants in shared memory, [KAP][32] from the first of them, the same for every
 // lane) and the packed slots.
 __device__ __forceinline__ void dg_consume4(uint32_t taddr, const int32_t* __restrict__ kap,
                                             uint32_t release, uint4 (&out)[2]) {
     uint32_t d[dg::NW][4];
 #pragma unroll
-    for (int w = 0; w < dg::NW; ++w) tm_ld4(taddr + (uint32_t)(16 * w), d[w]);
+    for (int w = 0; w < dg::NW; ++w) tm_ld4(taddr + (uint32_t)(32 * w), d[w]);
     asm volatile("tcgen05.wait::ld.sync.aligned;"
                  : "+r"(d[0][0]), "+r"(d[0][1]), "+r"(d[0][2]), "+r"(d[0][3]), "+r"(d[1][0]),
                    "+r"(d[1][1]), "+r"(d[1][2]), "+r"(d[1][3]), "+r"(d[2][0]), "+r"(d[2][1]),
@@ -117,8 +119,10 @@ __device__ __forceinline__ void dg_consume4(uint32_t taddr, const int32_t* __res
                  : "memory");
     asm volatile("" : "+r"(d[8][0]), "+r"(d[8][1]), "+r"(d[8][2]), "+r"(d[8][3]), "+r"(d[9][0]),
                       "+r"(d[9][1]), "+r"(d[9][2]), "+r"(d[9][3])::"memory");
-    tc::fence_before_sync();
-    dg_arrive(release);
+    if (release) {
+        tc::fence_before_sync();
+        dg_arrive(release);
+    }
     // the four chains run position by position; kap is [KAP][32] in shared memory, so one 16-byte
     // load gives constant i of the thread's four outputs
     const int4* k4 = reinterpret_cast<const int4*>(kap);
@@ -191,10 +195,8 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
             mbar_init(b_afull + 8 * s, DG_M);
             mbar_init(b_aempty + 8 * s, 1);
         }
-        for (int s = 0; s < 3; ++s) {
-            mbar_init(b_accfull + 8 * s, 1);
-            mbar_init(b_accempty + 8 * s, DG_CONSUMERS);
-        }
+        mbar_init(b_accfull, 1);
+        mbar_init(b_accempty, DG_CONSUMERS);
         mbar_init(b_drain, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -230,38 +232,36 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
             const uint64_t b_desc0 = tc::smem_desc(smem_u32(sB), 128, DG_SBO_B);
             const uint64_t one_desc = tc::smem_desc(smem_u32(sOne), 128, DG_SBO_SEED);
             const uint64_t magic_desc = tc::smem_desc(smem_u32(sMagic), 128, DG_SBO_SEED);
-            for (uint64_t t = 0; t < 2 * nmine; ++t) {
-                const uint64_t it = t >> 1;
-                const int q = (int)(t & 1), s = (int)(it & 1), ai = (int)(t % 3);
-                if (q == 0 && !mbar_wait_bounded(b_afull + 8 * s, (uint32_t)((it >> 1) & 1), DG_WAIT_LIMIT)) {
+            for (uint64_t it = 0; it < nmine; ++it) {
+                const int s = (int)(it & 1);
+                if (!mbar_wait_bounded(b_afull + 8 * s, (uint32_t)((it >> 1) & 1), DG_WAIT_LIMIT)) {
                     fail_now(5);
                     break;
                 }
-                if (t >= 3 && !mbar_wait_bounded(b_accempty + 8 * ai, (uint32_t)(((t / 3) - 1) & 1),
-                                                  DG_WAIT_LIMIT)) {
+                if (it >= 1 && !mbar_wait_bounded(b_accempty, (uint32_t)((it - 1) & 1), DG_WAIT_LIMIT)) {
                     fail_now(6);
                     break;
                 }
                 if (aborted()) break;
                 tc::fence_after_sync();
-                const uint32_t acc = tmem + DG_ACC_COLS * (uint32_t)ai;
+                const uint32_t acc = tmem;
                 // descriptors: base + the operand's byte offset / 16 (the start-address field)
                 const uint64_t ad0 = a_desc0 + (uint64_t)((s * DG_A_BYTES) >> 4);
-                const uint64_t bd0 = b_desc0 + (uint64_t)((q * DG_B_CHUNK) >> 4);
-                tc::mma_bf16(acc, one_desc, magic_desc, tc::idesc_bf16(DG_M, (int)DG_ACC_COLS), 0u);
+                tc::mma_bf16(acc, one_desc, magic_desc, tc::idesc_bf16(DG_M, (int)DG_SEED_N), 0u);
+                tc::mma_bf16(acc + DG_SEED_N, one_desc, magic_desc, tc::idesc_bf16(DG_M, (int)DG_SEED_N), 0u);
 #pragma unroll
                 for (int k = 0; k < dg::NSTEPS; ++k) {
                     const dg::MmaStep ms = dg::mma_step(k);
-                    const uint32_t idesc = tc::idesc_bf16(DG_M, 16 * (ms.jend - ms.jmin));
+                    const uint32_t idesc = tc::idesc_bf16(DG_M, 32 * (ms.jend - ms.jmin));
 #pragma unroll
                     for (int kk = 0; kk < 2; ++kk)
-                        tc::mma_bf16(acc + (uint32_t)(16 * (ms.i + ms.jmin - dg::WMIN)),
+                        tc::mma_bf16(acc + (uint32_t)(32 * (ms.i + ms.jmin - dg::WMIN)),
                                      ad0 + (uint64_t)(((4 * ms.i + 2 * kk) * 128) >> 4),
-                                     bd0 + (uint64_t)((ms.jmin * 1024 + kk * 256) >> 4), idesc, 1u);
+                                     b_desc0 + (uint64_t)((ms.jmin * 2048 + kk * 256) >> 4), idesc, 1u);
                 }
                 issued = true;
-                tc::commit(b_accfull + 8 * ai);
-                if (q == 1) tc::commit(b_aempty + 8 * s);
+                tc::commit(b_accfull);
+                tc::commit(b_aempty + 8 * s);
             }
             if (issued) {  // every MMA completed before the tensor memory is freed
                 tc::commit(b_drain);
@@ -328,25 +328,21 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
         const int r = 32 * quad + lane;
         for (uint64_t it = 0; it < nmine; ++it) {
             const uint64_t base = tile_base(blockIdx.x + it * gridDim.x, r);
+            if (!mbar_wait_bounded(b_accfull, (uint32_t)(it & 1), DG_WAIT_LIMIT)) {
+                fail_now(9);
+                break;
+            }
+            if (aborted()) break;
+            tc::fence_after_sync();
 #pragma unroll 1
-            for (int q = 0; q < 2; ++q) {
-                const uint64_t t = 2 * it + (uint64_t)q;
-                const int ai = (int)(t % 3);
-                if (!mbar_wait_bounded(b_accfull + 8 * ai, (uint32_t)((t / 3) & 1), DG_WAIT_LIMIT)) {
-                    fail_now(9);
-                    goto consumers_done;
-                }
-                if (aborted()) goto consumers_done;
-                tc::fence_after_sync();
-                const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + DG_ACC_COLS * (uint32_t)ai +
-                                       (uint32_t)(4 * sub);
+            for (int q = 0; q < 2; ++q) {  // output reals 16 q + 4 sub ..; the second releases
+                const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(16 * q + 4 * sub);
                 uint4 out[2];
-                dg_consume4(taddr, skap + 16 * q + 4 * sub, b_accempty + 8 * ai, out);
+                dg_consume4(taddr, skap + 16 * q + 4 * sub, q == 1 ? b_accempty : 0u, out);
                 st[base | slot_off(8 * q + 2 * sub)] = out[0];
                 st[base | slot_off(8 * q + 2 * sub + 1)] = out[1];
             }
         }
-    consumers_done:;
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -513,11 +509,11 @@ bool dg_build_image(const std::complex<double> M[16][16], uint32_t* bimg, int32_
             if (b >= dg::DBOUND) return false;
         }
     }
-    // B: chunk q = c / 16, row 16 j + c % 16, K = input real k
+    // B: row 32 j + c (digit j of output real c), K = input real k
     for (int c = 0; c < 32; ++c)
         for (int j = 0; j < dg::DIGITS; ++j)
             for (int k = 0; k < 32; ++k)
-                h16[((c / 16) * DG_B_CHUNK + dg::op_off(16 * j + c % 16, k, DG_SBO_B)) / 2] =
+                h16[dg::op_off(32 * j + c, k, DG_SBO_B) / 2] =
                     dg_bf16(rho[k][c][j]);
     // carry constants: K_c = 2^111 + 2^55 - (2^55 + 128 G) S_c, taken mod 2^112
     i128 G = 0;

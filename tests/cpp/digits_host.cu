@@ -70,7 +70,7 @@ static double run_tile(const cdd M[16][16], const uint32_t* bimg, const int32_t 
     // matrix digits back from the B image
     auto rho = [&](int k, int c, int j) {
         const uint16_t* h16 = reinterpret_cast<const uint16_t*>(bimg);
-        return (int64_t)bf16_to_f(h16[((c / 16) * DG_B_CHUNK + dg::op_off(16 * j + c % 16, k, DG_SBO_B)) / 2]);
+        return (int64_t)bf16_to_f(h16[dg::op_off(32 * j + c, k, DG_SBO_B) / 2]);
     };
     // the MMA steps: integer sums per weight (the tensor cores' F32 accumulation is exact below 2^24)
     int64_t D[32][dg::NW];
