@@ -10,25 +10,23 @@
 // accumulation) and the CUDA cores only permute bytes into BF16 operands (8 byte permutes per
 // amplitude) and run the carry chains (about 70 operations per amplitude).
 //
-// k_dg2: one CTA per SM, persistent over blocks of 128 tiles (2048 amplitudes), warp-specialised:
-//   warp 0      lane 0 issues the MMAs of a block into the one 320-column tensor-memory accumulator
-//               (10 weights x 32 output reals): two seed MMAs (every column := 1.5 * 2^23), then for
-//               each digit i one MMA per K half over the matrix digits j it pairs with (M = 128 tiles,
-//               K = 16, N = 32 per digit, up to 256); A comes from tensor memory, B from shared memory;
-//   warps 1-4   converters, thread = tile row = tensor-memory lane: coalesced cp.async copies of the
-//               block's slots (digit layout) into one of four shared-memory stages, three blocks
-//               ahead; then each thread byte-permutes its row's 16 slots into the A operand in tensor
-//               memory (K = 8 digits x 32 reals, BF16);
-//   warps 5-20  consumers: each thread one tile row and 8 output reals (4 amplitudes): their 10
-//               weights from tensor memory (all loads, then one wait), the carry chains, the packed
-//               digits written into the block's stage; then every consumer copies 4 slots of the
-//               stage to global memory, coalesced.
-// Hand-offs are mbarriers: a_full (128 converters), a_empty / acc_full (MMA commits), acc_empty
-// (512 consumers, once their tensor-memory loads completed), and per stage ld_ready (128),
-// out_ready and free (512). Every wait is bounded: a wait that runs out sets the error word and an
-// abort flag that stops every role; the MMA thread drains its MMAs (bounded) before the CTA frees
-// its tensor memory. Shared memory per block: B read by the MMAs (100 KB), the stage written and
-// read twice (128 KB); the A operand never touches shared memory.
+// k_dg2: one CTA per SM, persistent over blocks of 128 tiles, warp-specialised:
+//   warp 0      lane 0 issues the MMAs of a block into the one 320-column accumulator (10 weights
+//               x 32 output reals): two seed MMAs (every column := 1.5 * 2^23), then for each digit
+//               i of A one MMA per K half over the matrix digits j it pairs with (M = 128 tiles,
+//               K = 16, N = 32 per digit, up to 256), so every A slice is read once per block;
+//   warps 1-4   converters, one tile row each: copy the tile's 16 slots (digit layout) to shared
+//               memory with cp.async two blocks ahead, byte-permute them into the A operand
+//               (K = 8 digits x 32 reals, BF16) of one of two buffers;
+//   warps 5-20  consumers: every block, each thread one tile row and output reals 4 s .. 4 s + 3 and
+//               16 + 4 s .. 16 + 4 s + 3: read their 10 weights from tensor memory (all loads, then
+//               one wait), run the carry chains, pack the digits and store the 4 amplitudes.
+// Hand-offs are mbarriers: a_full[2] (128 converter arrivals), a_empty[2] (MMA commit after the
+// block), acc_full (MMA commit), acc_empty (512 consumer arrivals once their tensor-memory loads
+// completed). Every wait is bounded: a wait that runs out sets the error word and an abort flag
+// that stops every role; the MMA thread drains its MMAs (bounded) before the CTA frees its
+// tensor memory. Shared memory per block read by the tensor cores: A 80 KB, B 100 KB (the chunked
+// form, which re-read A per 16 outputs, was bound by shared-memory bandwidth).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -46,45 +44,30 @@ namespace qgpu {
 
 constexpr int DG_M = 128;                               // tiles per block (MMA rows)
 constexpr int DG_THREADS = 672;                         // 21 warps: 6 on some SM sub-partition, so 80 registers
-constexpr int DG_CONVERTERS = 128;                      // warps 1-4
-constexpr int DG_CONSUMERS = 512;                       // warps 5-20
+constexpr int DG_K = 256;                               // A: 8 digits x 32 reals
+constexpr uint32_t DG_SBO_A = (DG_K / 8) * 128;         // 4096: 8-row groups of A
+constexpr uint32_t DG_A_BYTES = DG_M * DG_K * 2;        // 64 KB per buffer
 constexpr uint32_t DG_SBO_B = (32 / 8) * 128;           // 512: 8-row groups of B (K = 32)
 constexpr uint32_t DG_B_BYTES = 256 * 32 * 2;           // 16 KB: rows 32 j + c (8 digits x 32 outputs)
-constexpr uint32_t DG_SBO_SEED = (16 / 8) * 128;        // 256: 8-row groups of the K = 16 seed B
-constexpr uint32_t DG_SEED_N = 160;                     // two seed MMAs of N = 160
-constexpr uint32_t DG_MAGIC_BYTES = DG_SEED_N * 16 * 2;  // 5 KB: B of the seed MMA (MAGIC_F at k = 0)
-constexpr int DG_NSTAGE = 4;                            // staging buffers (loads, then the outputs)
-constexpr uint32_t DG_STAGE_BYTES = DG_M * 16 * 16;     // 32 KB: one block's 2048 slots
-// tensor memory: the accumulator (10 weights x 32 output reals, weight-major), the A operand
-// (K = 8 digits x 32 reals in BF16 pairs: column 16 i + slot holds digit i of the slot's real and
-// imaginary parts) and the seed MMA's A (a ones column)
-constexpr uint32_t DG_ACC_COLS = 32 * dg::NW;           // 320
-constexpr uint32_t DG_A_COL = DG_ACC_COLS;              // 128 columns
-constexpr uint32_t DG_SEED_COL = DG_A_COL + 128;        // 8 columns
+constexpr uint32_t DG_ACC_COLS = 32 * dg::NW;           // 320 columns: weight-major, 32 outputs each
 constexpr uint32_t DG_TCOLS = 512;
-constexpr int DG_NBARS = 5 + 3 * DG_NSTAGE;
-constexpr size_t DG_SMEM = DG_B_BYTES + DG_MAGIC_BYTES + DG_NSTAGE * DG_STAGE_BYTES + 1024 + 32 * dg::KAP * 4;
+constexpr int DG_CONSUMERS = 512;                       // 16 consumer warps
+constexpr uint32_t DG_STAGE_BYTES = DG_M * 16 * 16;    // 32 KB: one block's slots
+constexpr uint32_t DG_SBO_SEED = (16 / 8) * 128;      // 256: 8-row groups of the K = 16 seed operands
+constexpr uint32_t DG_ONE_BYTES = DG_M * 16 * 2;        // 4 KB: A of the seed MMA (a ones column)
+constexpr uint32_t DG_SEED_N = DG_ACC_COLS / 2;         // two seed MMAs of N = 160
+constexpr uint32_t DG_MAGIC_BYTES = DG_SEED_N * 16 * 2;  // 5 KB: B of the seed MMA (MAGIC_F row)
+constexpr size_t DG_SMEM = 2 * DG_A_BYTES + DG_B_BYTES + 2 * DG_STAGE_BYTES + DG_ONE_BYTES +
+                           DG_MAGIC_BYTES + 2048 + 32 * dg::KAP * 4;
 constexpr uint32_t DG_WAIT_LIMIT = 1u << 22;
 
-// A block is the 2048 amplitudes of 128 tiles: index bits = the 4 tile bits and the 7 lowest
-// other bits (the rows); they always include bits 0..6. Its "local index" numbers them in index
-// order (the 11 bits compressed, ascending), so local index 128 k + t lies at global offset
-// koff[k] + t from the block's base: 16 runs of at least 128 contiguous amplitudes. Row r, slot j
-// is local index rloc(r) | jloc[j] (rloc: r's bits at the rows' local positions rpos[]).
 struct DgArgs {
     uint64_t nblocks;                  // dim / 16 / 128
     int bits[4];                       // tile bits, ascending (slot bit m <-> bits[m])
     int* err;
-    int32_t jloc[16];                  // local index of slot j in row 0
-    int32_t rpos[7];                   // local position of row bit b
-    int64_t koff[16];                  // global offset of local index 128 k
     int32_t kap[32][dg::KAP];          // carry constants per output real
-    uint32_t bimg[DG_B_BYTES / 4];     // matrix digits, shared-memory layout
+    uint32_t bimg[DG_B_BYTES / 4];     // matrix digits, both chunks, shared-memory layout
 };
-
-// staging buffers hold local index l at 16-byte position l ^ ((l >> 4) & 7): conflict-free for
-// coalesced copies (consecutive l) and for rows read or written slot by slot
-__device__ __forceinline__ uint32_t dg_swz(uint32_t l) { return l ^ ((l >> 4) & 7u); }
 
 // ---- tensor-memory loads without the wait (the wait names the registers it completes) ------
 __device__ __forceinline__ void tm_ld16(uint32_t taddr, uint32_t (&r)[16]) {
@@ -178,73 +161,63 @@ __device__ __forceinline__ void dg_consume4(uint32_t taddr, const int32_t* __res
     for (int u = 0; u < 2; ++u) out[u] = make_uint4(w4[u][0], w4[u][1], w4[u][2], w4[u][3]);
 }
 
-__device__ __forceinline__ void tm_st8(uint32_t taddr, const uint32_t (&v)[8]) {
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
-                 "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
-                 : "memory");
-}
-// D[tmem] (+)= A[tmem] * B[smem]; one thread issues.
-__device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
-                                       uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
 __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
                                                        const __grid_constant__ DgArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
-    uint8_t* sB = sm;
-    uint8_t* sMagic = sB + DG_B_BYTES;
-    uint8_t* sStage = sMagic + DG_MAGIC_BYTES;
-    uint8_t* tail = sStage + DG_NSTAGE * DG_STAGE_BYTES;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(tail);
-    uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 8 * DG_NBARS);
-    int* abort_flag = reinterpret_cast<int*>(tail + 8 * DG_NBARS + 4);
-    int32_t* skap = reinterpret_cast<int32_t*>(tail + 1024);  // carry constants [KAP][32]
+    uint8_t* sA = sm;
+    uint8_t* sB = sm + 2 * DG_A_BYTES;
+    uint8_t* sStage = sB + DG_B_BYTES;  // 2 x 32 KB: converters' staging of the state
+    uint8_t* sOne = sStage + 2 * DG_STAGE_BYTES;
+    uint8_t* sMagic = sOne + DG_ONE_BYTES;
+    uint8_t* tail = sMagic + DG_MAGIC_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(tail);  // a_full[2] a_empty[2] acc_full[3] acc_empty[3] drain
+    uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 128);
+    int* abort_flag = reinterpret_cast<int*>(tail + 132);
+    int32_t* skap = reinterpret_cast<int32_t*>(tail + 2048);  // carry constants [KAP][32]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // a_full, a_empty, acc_full, acc_empty, drain, then per stage: ld_ready, out_ready, free
-    const uint32_t b_afull = smem_u32(bars), b_aempty = smem_u32(bars + 1), b_accfull = smem_u32(bars + 2),
-                   b_accempty = smem_u32(bars + 3), b_drain = smem_u32(bars + 4);
-    auto b_ldready = [&](int s) { return smem_u32(bars + 5 + s); };
-    auto b_outready = [&](int s) { return smem_u32(bars + 5 + DG_NSTAGE + s); };
-    auto b_free = [&](int s) { return smem_u32(bars + 5 + 2 * DG_NSTAGE + s); };
+    const uint32_t b_afull = smem_u32(bars), b_aempty = smem_u32(bars + 2),
+                   b_accfull = smem_u32(bars + 4), b_accempty = smem_u32(bars + 7),
+                   b_drain = smem_u32(bars + 10);
 
     for (int i = tid; i < (int)(DG_B_BYTES / 4); i += DG_THREADS)
         reinterpret_cast<uint32_t*>(sB)[i] = a.bimg[i];
     for (int i = tid; i < 32 * dg::KAP; i += DG_THREADS) skap[i] = a.kap[i % 32][i / 32];
-    for (int i = tid; i < (int)(DG_MAGIC_BYTES / 2); i += DG_THREADS) {  // MAGIC_F at k = 0 of every row
-        const int row = i / 16, k = i % 16;
-        *reinterpret_cast<uint16_t*>(sMagic + dg::op_off(row, k, DG_SBO_SEED)) = k == 0 ? 0x4B40 : 0;
+    // seed operands: A = e_0 in every row (BF16 1.0 at k = 0), B = MAGIC_F at k = 0 in every row
+    for (int i = tid; i < (int)((DG_ONE_BYTES + DG_MAGIC_BYTES) / 2); i += DG_THREADS) {
+        const bool one = i < (int)(DG_ONE_BYTES / 2);
+        const int e = one ? i : i - (int)(DG_ONE_BYTES / 2);
+        const int row = e / 16, k = e % 16;
+        const uint16_t v = k != 0 ? 0 : (one ? 0x3F80 : 0x4B40);  // BF16 1.0 / 1.5 * 2^23
+        *reinterpret_cast<uint16_t*>((one ? sOne : sMagic) + dg::op_off(row, k, DG_SBO_SEED)) = v;
     }
     if (tid == 0) {
-        mbar_init(b_afull, DG_CONVERTERS);
-        mbar_init(b_aempty, 1);
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(b_afull + 8 * s, DG_M);
+            mbar_init(b_aempty + 8 * s, 1);
+        }
         mbar_init(b_accfull, 1);
         mbar_init(b_accempty, DG_CONSUMERS);
         mbar_init(b_drain, 1);
-        for (int s = 0; s < DG_NSTAGE; ++s) {
-            mbar_init(b_ldready(s), DG_CONVERTERS);
-            mbar_init(b_outready(s), DG_CONSUMERS);
-            mbar_init(b_free(s), DG_CONSUMERS);
-        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tc::alloc(smem_u32(slot), DG_TCOLS);
-    fence_proxy_async_shared();  // B and the seed B (generic-proxy writes) visible to the MMAs
+    fence_proxy_async_shared();  // B (generic-proxy writes) visible to the MMAs
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *slot;
     const uint64_t nmine =
         (a.nblocks > blockIdx.x) ? (a.nblocks - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
-    auto block_base = [&](uint64_t it) {
-        const uint64_t blk = blockIdx.x + it * gridDim.x;
-        return insert_zero(insert_zero(insert_zero(insert_zero(blk * DG_M, a.bits[0]), a.bits[1]), a.bits[2]),
-                           a.bits[3]);
+    const uint64_t o0 = 1ull << a.bits[0], o1 = 1ull << a.bits[1], o2 = 1ull << a.bits[2],
+                   o3 = 1ull << a.bits[3];
+    auto slot_off = [&](int j) {
+        return ((j & 1) ? o0 : 0) | ((j & 2) ? o1 : 0) | ((j & 4) ? o2 : 0) | ((j & 8) ? o3 : 0);
+    };
+    auto tile_base = [&](uint64_t blk, int r) {
+        return insert_zero(
+            insert_zero(insert_zero(insert_zero(blk * DG_M + r, a.bits[0]), a.bits[1]), a.bits[2]),
+            a.bits[3]);
     };
     auto fail_now = [&](int code) {
         atomicExch(a.err, code);
@@ -255,10 +228,13 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
     if (warp == 0) {  // ------------------------------------------------------------ MMA issue
         if (lane == 0) {
             bool issued = false;
+            const uint64_t a_desc0 = tc::smem_desc(smem_u32(sA), 128, DG_SBO_A);
             const uint64_t b_desc0 = tc::smem_desc(smem_u32(sB), 128, DG_SBO_B);
+            const uint64_t one_desc = tc::smem_desc(smem_u32(sOne), 128, DG_SBO_SEED);
             const uint64_t magic_desc = tc::smem_desc(smem_u32(sMagic), 128, DG_SBO_SEED);
             for (uint64_t it = 0; it < nmine; ++it) {
-                if (!mbar_wait_bounded(b_afull, (uint32_t)(it & 1), DG_WAIT_LIMIT)) {
+                const int s = (int)(it & 1);
+                if (!mbar_wait_bounded(b_afull + 8 * s, (uint32_t)((it >> 1) & 1), DG_WAIT_LIMIT)) {
                     fail_now(5);
                     break;
                 }
@@ -269,21 +245,23 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
                 if (aborted()) break;
                 tc::fence_after_sync();
                 const uint32_t acc = tmem;
-                mma_ts(acc, tmem + DG_SEED_COL, magic_desc, tc::idesc_bf16(DG_M, (int)DG_SEED_N), 0u);
-                mma_ts(acc + DG_SEED_N, tmem + DG_SEED_COL, magic_desc, tc::idesc_bf16(DG_M, (int)DG_SEED_N), 0u);
+                // descriptors: base + the operand's byte offset / 16 (the start-address field)
+                const uint64_t ad0 = a_desc0 + (uint64_t)((s * DG_A_BYTES) >> 4);
+                tc::mma_bf16(acc, one_desc, magic_desc, tc::idesc_bf16(DG_M, (int)DG_SEED_N), 0u);
+                tc::mma_bf16(acc + DG_SEED_N, one_desc, magic_desc, tc::idesc_bf16(DG_M, (int)DG_SEED_N), 0u);
 #pragma unroll
                 for (int k = 0; k < dg::NSTEPS; ++k) {
                     const dg::MmaStep ms = dg::mma_step(k);
                     const uint32_t idesc = tc::idesc_bf16(DG_M, 32 * (ms.jend - ms.jmin));
 #pragma unroll
                     for (int kk = 0; kk < 2; ++kk)
-                        mma_ts(acc + (uint32_t)(32 * (ms.i + ms.jmin - dg::WMIN)),
-                               tmem + DG_A_COL + (uint32_t)(16 * ms.i + 8 * kk),
-                               b_desc0 + (uint64_t)((ms.jmin * 2048 + kk * 256) >> 4), idesc, 1u);
+                        tc::mma_bf16(acc + (uint32_t)(32 * (ms.i + ms.jmin - dg::WMIN)),
+                                     ad0 + (uint64_t)(((4 * ms.i + 2 * kk) * 128) >> 4),
+                                     b_desc0 + (uint64_t)((ms.jmin * 2048 + kk * 256) >> 4), idesc, 1u);
                 }
                 issued = true;
                 tc::commit(b_accfull);
-                tc::commit(b_aempty);
+                tc::commit(b_aempty + 8 * s);
             }
             if (issued) {  // every MMA completed before the tensor memory is freed
                 tc::commit(b_drain);
@@ -292,96 +270,64 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
         }
         __syncwarp();
     } else if (warp <= 4) {  // ------------------------------------------------------ converters
-        // Thread r = tile row r = tensor-memory lane r. Loads: coalesced cp.async copies of the
-        // block's 2048 slots (local index 128 k + r) into a stage, NSTAGE - 1 blocks ahead; then
-        // each thread byte-permutes its row's 16 slots into the A operand in tensor memory.
-        const int r = 32 * (warp & 3) + lane;
-        const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-        uint32_t rloc = 0;
-#pragma unroll
-        for (int b = 0; b < 7; ++b) rloc |= (uint32_t)((r >> b) & 1) << a.rpos[b];
-        {  // the seed MMA's A: BF16 1.0 at k = 0 of every row, zeros elsewhere
-            const uint32_t one[8] = {0x3F80u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-            tm_st8(tmem + lane_base + DG_SEED_COL, one);
-            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-        }
+        // Each thread copies its tile row's 16 slots global -> shared with cp.async into one of two
+        // stages (slot j of row r at stage[j * 128 + r]: conflict-free for the warp), two blocks
+        // ahead of the block it converts, so no registers are held while the loads fly.
+        const int r = tid - 32;
         auto issue = [&](uint64_t it) {
-            const uint4* src = st + block_base(it) + r;
-            uint8_t* dst = sStage + (uint32_t)(it % DG_NSTAGE) * DG_STAGE_BYTES;
+            const uint64_t b0 = tile_base(blockIdx.x + it * gridDim.x, r);
+            uint8_t* dst = sStage + (uint32_t)(it & 1) * DG_STAGE_BYTES;
 #pragma unroll
-            for (int k = 0; k < 16; ++k)
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst + dg_swz(128 * k + r) * 16)),
-                             "l"(src + a.koff[k])
+            for (int j = 0; j < 16; ++j)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst + (j * DG_M + r) * 16)),
+                             "l"(st + (b0 | slot_off(j)))
                              : "memory");
         };
-        for (int p = 0; p < DG_NSTAGE - 1; ++p) {
-            if ((uint64_t)p < nmine) issue(p);
-            asm volatile("cp.async.commit_group;" ::: "memory");
-        }
+        if (nmine > 0) issue(0);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        if (nmine > 1) issue(1);
+        asm volatile("cp.async.commit_group;" ::: "memory");
         for (uint64_t it = 0; it < nmine; ++it) {
-            const int s = (int)(it % DG_NSTAGE);
-            asm volatile("cp.async.wait_group %0;" ::"n"(DG_NSTAGE - 2) : "memory");  // block it's copies
-            dg_arrive(b_ldready(s));
-            if (!mbar_wait_bounded(b_ldready(s), (uint32_t)((it / DG_NSTAGE) & 1), DG_WAIT_LIMIT)) {
-                fail_now(8);
-                break;
-            }
-            if (it >= 1 && !mbar_wait_bounded(b_aempty, (uint32_t)((it - 1) & 1), DG_WAIT_LIMIT)) {
+            const int s = (int)(it & 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");  // block it's group is complete
+            if (it >= 2 && !mbar_wait_bounded(b_aempty + 8 * s, (uint32_t)(((it >> 1) - 1) & 1), DG_WAIT_LIMIT)) {
                 fail_now(8);
                 break;
             }
             if (aborted()) break;
-            tc::fence_after_sync();
-            const uint8_t* stage = sStage + (uint32_t)s * DG_STAGE_BYTES;
+            const uint8_t* src = sStage + (uint32_t)s * DG_STAGE_BYTES;
+            uint8_t* A = sA + (uint32_t)s * DG_A_BYTES;
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {  // slots 8h..8h+7
-                uint4 v[8];
+            for (int g = 0; g < 4; ++g) {  // slots 4g..4g+3: one 16-byte row of each digit's core matrix
+                uint4 v[4];
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    v[q] = *reinterpret_cast<const uint4*>(stage + dg_swz(rloc | (uint32_t)a.jloc[8 * h + q]) * 16);
+                for (int q = 0; q < 4; ++q) v[q] = *reinterpret_cast<const uint4*>(src + ((4 * g + q) * DG_M + r) * 16);
 #pragma unroll
                 for (int i = 0; i < dg::DIGITS; ++i) {
-                    uint32_t w[8];
+                    uint32_t w[4];
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) {
+                    for (int q = 0; q < 4; ++q) {
                         const uint32_t sw = (i >> 1) == 0 ? v[q].x : (i >> 1) == 1 ? v[q].y : (i >> 1) == 2 ? v[q].z : v[q].w;
                         w[q] = dg::a_word(sw, i & 1);
                     }
-                    tm_st8(tmem + lane_base + DG_A_COL + (uint32_t)(16 * i + 8 * h), w);
+                    *reinterpret_cast<uint4*>(A + dg::op_off(r, 32 * i + 8 * g, DG_SBO_A)) =
+                        make_uint4(w[0], w[1], w[2], w[3]);
                 }
             }
-            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-            tc::fence_before_sync();
-            dg_arrive(b_afull);
-            // refill the stage block it - 1 used, once its outputs went out
-            const uint64_t nx = it + DG_NSTAGE - 1;
-            if (nx < nmine) {
-                if (nx >= (uint64_t)DG_NSTAGE &&
-                    !mbar_wait_bounded(b_free((int)(nx % DG_NSTAGE)), (uint32_t)(((nx / DG_NSTAGE) - 1) & 1),
-                                       DG_WAIT_LIMIT)) {
-                    fail_now(8);
-                    break;
-                }
-                issue(nx);
-            }
+            fence_proxy_async_shared();  // the generic-proxy writes of A visible to the MMAs
+            dg_arrive(b_afull + 8 * s);
+            if (it + 2 < nmine) issue(it + 2);  // refills the stage just read
             asm volatile("cp.async.commit_group;" ::: "memory");
         }
         asm volatile("cp.async.wait_group 0;" ::: "memory");  // nothing in flight at exit
     } else {  // ------------------------------------------------------------------- consumers
-        // warp 5 + 4 sub + k: tensor-memory lanes 32 (warp % 4) (the tile rows it may read), output
-        // reals 4 sub .. 4 sub + 3 and 16 + 4 sub .. (amplitudes 2 sub, 2 sub + 1, 8 + 2 sub, 9 + 2 sub).
-        // Results go to the block's stage; once every consumer wrote, each copies 4 slots out,
-        // coalesced (local index 512 i + ct).
+        // warp 5 + 4 sub + k: tensor-memory lanes 32 (warp % 4) (the tile rows it may read) and
+        // output reals 4 sub .. 4 sub + 3 of every job's chunk (amplitudes 2 sub, 2 sub + 1)
         const int sub = (warp - 5) >> 2;
         const int quad = warp & 3;
         const int r = 32 * quad + lane;
-        const int ct = tid - 32 * 5;
-        uint32_t rloc = 0;
-#pragma unroll
-        for (int b = 0; b < 7; ++b) rloc |= (uint32_t)((r >> b) & 1) << a.rpos[b];
         for (uint64_t it = 0; it < nmine; ++it) {
-            const int s = (int)(it % DG_NSTAGE);
-            uint8_t* stage = sStage + (uint32_t)s * DG_STAGE_BYTES;
+            const uint64_t base = tile_base(blockIdx.x + it * gridDim.x, r);
             if (!mbar_wait_bounded(b_accfull, (uint32_t)(it & 1), DG_WAIT_LIMIT)) {
                 fail_now(9);
                 break;
@@ -393,22 +339,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1) k_dg2(uint4* __restrict__ st,
                 const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(16 * q + 4 * sub);
                 uint4 out[2];
                 dg_consume4(taddr, skap + 16 * q + 4 * sub, q == 1 ? b_accempty : 0u, out);
-#pragma unroll
-                for (int u = 0; u < 2; ++u)
-                    *reinterpret_cast<uint4*>(stage + dg_swz(rloc | (uint32_t)a.jloc[8 * q + 2 * sub + u]) * 16) = out[u];
+                st[base | slot_off(8 * q + 2 * sub)] = out[0];
+                st[base | slot_off(8 * q + 2 * sub + 1)] = out[1];
             }
-            dg_arrive(b_outready(s));
-            if (!mbar_wait_bounded(b_outready(s), (uint32_t)((it / DG_NSTAGE) & 1), DG_WAIT_LIMIT)) {
-                fail_now(9);
-                break;
-            }
-            uint4* dst = st + block_base(it);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const uint32_t l = 512u * i + (uint32_t)ct;
-                dst[a.koff[l >> 7] + (l & 127u)] = *reinterpret_cast<const uint4*>(stage + dg_swz(l) * 16);
-            }
-            dg_arrive(b_free(s));
         }
     }
     tc::fence_before_sync();
@@ -626,29 +559,6 @@ int dg_launch_pass(qgpu_handle* h, const int bits[4], const uint32_t* bimg,
     DgArgs a;
     a.nblocks = (h->dim >> 4) / DG_M;
     for (int m = 0; m < 4; ++m) a.bits[m] = bits[m];
-    // block bits: the tile bits and the 7 lowest other bits (the rows), ascending
-    int rows[7], nr = 0, blockbits[11];
-    for (int q = 0; nr < 7; ++q)
-        if (q != bits[0] && q != bits[1] && q != bits[2] && q != bits[3]) rows[nr++] = q;
-    {
-        int nb = 0;
-        for (int q = 0; q < 7; ++q) blockbits[nb++] = rows[q];
-        for (int m = 0; m < 4; ++m) blockbits[nb++] = bits[m];
-        std::sort(blockbits, blockbits + 11);
-    }
-    auto rank = [&](int bit) { return (int)(std::find(blockbits, blockbits + 11, bit) - blockbits); };
-    for (int j = 0; j < 16; ++j) {
-        a.jloc[j] = 0;
-        for (int m = 0; m < 4; ++m)
-            if ((j >> m) & 1) a.jloc[j] |= 1 << rank(bits[m]);
-    }
-    for (int b = 0; b < 7; ++b) a.rpos[b] = rank(rows[b]);
-    for (int k = 0; k < 16; ++k) {  // local bits 7..10 are k's bits; bits 0..6 are index bits 0..6
-        int64_t off = 0;
-        for (int b = 0; b < 4; ++b)
-            if ((k >> b) & 1) off |= (int64_t)1 << blockbits[7 + b];
-        a.koff[k] = off;
-    }
     a.err = h->d_err;
     std::memcpy(a.kap, kap, sizeof(a.kap));
     std::memcpy(a.bimg, bimg, sizeof(a.bimg));
