@@ -539,14 +539,13 @@ bool dg_build_image(const std::complex<double> M[16][16], uint32_t* bimg, int32_
 }
 
 bool dg_supported(const qgpu_handle* h) {
-    static const int on = [] {
-        const char* e = std::getenv("QGPU_DIGITS");  // tuning knob: 0 keeps the float-pair kernels
-        return e ? std::atoi(e) : 1;
-    }();
-    static const int min_qubits = [] {  // tuning knob: smallest register that uses them
-        const char* e = std::getenv("QGPU_DIGITS_MIN_QUBITS");
-        return std::max(11, e ? std::atoi(e) : 11);
-    }();
+    // tuning knobs, read per call: QGPU_DIGITS=0 keeps the float-pair kernels; digit runs are
+    // used from QGPU_DIGITS_MIN_QUBITS qubits (default 20: below that the register sits in L2
+    // and the two layout conversions cost more than the passes save)
+    const char* e = std::getenv("QGPU_DIGITS");
+    const char* m = std::getenv("QGPU_DIGITS_MIN_QUBITS");
+    const int on = e ? std::atoi(e) : 1;
+    const int min_qubits = std::max(11, m ? std::atoi(m) : 20);
     return on != 0 && h->precision == QGPU_C128 && h->mode == QGPU_MODE_FAST &&
            (h->dim >> 4) % DG_M == 0 && h->n_qubits >= min_qubits;
 }

@@ -17,7 +17,9 @@ TOL = 1e-12
 
 
 @pytest.fixture(autouse=True)
-def _lib(gpu_lib):
+def _lib(gpu_lib, monkeypatch):
+    # digit runs from 11 qubits here (the default starts at 20), so small registers exercise them
+    monkeypatch.setenv("QGPU_DIGITS_MIN_QUBITS", "11")
     yield
 
 
