@@ -309,27 +309,54 @@ def run_precision(args) -> None:
 def run_batch_leg(args) -> None:
     """Batching configuration (a secondary line): independent ansatz circuits of 10..24 qubits,
     4 layers each, own angles and observables; energies + adjoint gradients for every circuit in
-    one qgpu_batch_run call. Reports circuits/s and the fusion budget tuned per size bucket."""
+    one qgpu_batch_run call per rank. Under torchrun the circuits shard across ranks by cost
+    (batch.shard) and the results come back with one all-reduce of flat arrays; the time is the
+    slowest rank's, between barriers. Reports circuits/s and the fusion budget tuned per size."""
+    import torch
+
     from quantr_gb300 import _native as nat
     from quantr_gb300 import batch as B
     from quantr_gb300 import gradients as GR
 
+    world, rank, local = dist_setup()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
     cs = B.batch_config(count=args.batch_count)
     sizes = {}
     for c in cs:
         sizes[c.n] = sizes.get(c.n, 0) + 1
-    out = {"impl": "ours", "config": "batch", "circuits": len(cs), "qubits_histogram": sizes,
-           "results": {}}
+    out = {"impl": "ours", "config": "batch", "circuits": len(cs), "n_gpus": world,
+           "qubits_histogram": sizes, "results": {}}
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
     for pname, prec in (("c128", nat.QGPU_C128), ("c64", nat.QGPU_C64)):
         B.run_batch(cs[:8], precision=prec)  # warm-up (module load, graph path)
+        tuned = {}
+
+        def runner(part, prec=prec):
+            e, g, t = B.run_batch(part, precision=prec)
+            tuned.update(t)
+            return e, g
+
+        barrier()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        e, g, tuned = B.run_batch(cs, precision=prec)
-        dt = time.perf_counter() - t0
+        e, g = B.run_distributed(cs, runner=runner)
+        torch.cuda.synchronize()
+        dt = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device=dev)
+        if world > 1:
+            torch.distributed.all_reduce(dt, op=torch.distributed.ReduceOp.MAX)
+        dt = float(dt.item())
         out["results"][pname] = {"seconds": dt, "circuits_per_s": len(cs) / dt,
                                  "tuned_ff_budget_per_qubits": tuned,
                                  "small_circuits_in_shared_memory": sum(
                                      1 for c in cs if c.n <= (12 if pname == "c128" else 13))}
-        if pname == "c128":
+        if pname == "c128" and rank == 0:
             rng = np.random.default_rng(0)
             worst = 0.0
             for i in rng.choice(len(cs), size=8, replace=False):
@@ -338,7 +365,8 @@ def run_batch_leg(args) -> None:
                 h.close()
                 worst = max(worst, abs(ei - e[i]), float(np.max(np.abs(gi - g[i]))))
             out["results"][pname]["max_abs_diff_vs_single_circuit_adjoint"] = worst
-    print(json.dumps(out), flush=True)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 def _sweep_worker(job):

@@ -7,7 +7,8 @@ SplitMix64 stream seeded 5 * 2^32 + i.
 
 Circuits are independent, so across GPUs they shard with no data-path collective:
 `shard(circuits, world)` balances the estimated cost 2^n * gates over ranks and
-`run_distributed` runs a rank's share and gathers (energy, gradient) pairs on every rank.
+`run_distributed` runs a rank's share and gathers (energy, gradient) pairs on every rank with one
+all-reduce of flat arrays.
 """
 from __future__ import annotations
 
@@ -105,7 +106,12 @@ def shard(circuits: list, world: int) -> list[list[int]]:
 
 
 def run_distributed(circuits: list[BatchCircuit], runner=None):
-    """Run this rank's share and gather every circuit's (energy, gradient) on all ranks."""
+    """Run this rank's share and gather every circuit's (energy, gradient) on all ranks.
+
+    The gather is one all-reduce (sum) of two flat float64 arrays, every circuit's energy and
+    its gradient slots written by the one rank that owns it and zero elsewhere: plain arrays, no
+    pickled objects (on the device for NCCL, on the host for gloo)."""
+    import torch
     import torch.distributed as dist
 
     world = dist.get_world_size() if dist.is_initialized() else 1
@@ -113,16 +119,19 @@ def run_distributed(circuits: list[BatchCircuit], runner=None):
     mine = shard(circuits, world)[rank]
     runner = runner or (lambda cs: run_batch(cs)[:2])
     e, g = runner([circuits[i] for i in mine]) if mine else (np.zeros(0), [])
-    local = list(zip(mine, [float(x) for x in e], g))
-    if world == 1:
-        gathered = [local]
-    else:
-        gathered = [None] * world
-        dist.all_gather_object(gathered, local)
+    offs = np.zeros(len(circuits) + 1, dtype=np.int64)
+    offs[1:] = np.cumsum([len(c.program.ops) for c in circuits])
     energies = np.zeros(len(circuits))
-    grads: list = [None] * len(circuits)
-    for part in gathered:
-        for i, ei, gi in part:
-            energies[i] = ei
-            grads[i] = gi
+    flat = np.zeros(int(offs[-1]))
+    for k, i in enumerate(mine):
+        energies[i] = e[k]
+        flat[offs[i]:offs[i + 1]] = g[k]
+    if world > 1:
+        dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" \
+            else torch.device("cpu")
+        buf = torch.from_numpy(np.concatenate([energies, flat])).to(dev)
+        dist.all_reduce(buf, op=dist.ReduceOp.SUM)
+        both = buf.cpu().numpy()
+        energies, flat = both[:len(circuits)], both[len(circuits):]
+    grads = [flat[offs[i]:offs[i + 1]].copy() for i in range(len(circuits))]
     return energies, grads

@@ -2,7 +2,7 @@
 
 Each rank evaluates its share with a CPU runner (the oracle plus numpy energies), standing in
 for the GPU runner; the test checks that every circuit lands exactly once and every rank ends
-with the same energies as a single-process run.
+with the same energies and gradient slots as a single-process run (one all-reduce of flat arrays).
 """
 import os
 import socket
@@ -26,7 +26,8 @@ def _cpu_runner(cs):
     from oracle import oracle as orc
 
     es = [W.energy_dense(orc.simulate(c.program, engine=orc.DENSE), c.a, c.b) for c in cs]
-    return np.array(es), [np.zeros(len(c.program.ops)) for c in cs]
+    # stand-in gradients that identify their circuit, so the gather of the gradient slots is checked
+    return np.array(es), [e + np.arange(len(c.program.ops)) * 1e-3 for e, c in zip(es, cs)]
 
 
 def _free_port() -> int:
@@ -42,6 +43,7 @@ def _worker(rank, world, port, out_dir):
     try:
         e, g = B.run_distributed(_circuits(), runner=_cpu_runner)
         np.save(os.path.join(out_dir, f"e{rank}.npy"), e)
+        np.save(os.path.join(out_dir, f"g{rank}.npy"), np.concatenate(g))
     finally:
         dist.destroy_process_group()
 
@@ -56,11 +58,12 @@ def test_shard_balances_and_covers():
 
 
 def test_two_rank_gather_matches_single_process(tmp_path):
-    ref, _ = _cpu_runner(_circuits())
+    ref, refg = _cpu_runner(_circuits())
     mp.spawn(_worker, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)
     for r in range(2):
         e = np.load(tmp_path / f"e{r}.npy")
         assert np.allclose(e, ref, atol=1e-12, rtol=0)
+        assert np.allclose(np.load(tmp_path / f"g{r}.npy"), np.concatenate(refg), atol=1e-12, rtol=0)
 
 
 def test_shard_meets_the_list_scheduling_bound():
