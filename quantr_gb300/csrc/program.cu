@@ -2006,6 +2006,33 @@ extern "C" int qgpu_apply_program(qgpu_handle* h, const qgpu_op* ops, size_t n_o
     int st = build_plan(ops, n_ops, h->n_qubits, mats, n_mat_doubles, none_flags, n_none_flags,
                         plan_options_for(h), &plan);
     if (st != QGPU_OK) return st;
+    // Fast mode carries f64 values as float pairs, which share the float32 exponent range: a
+    // program whose Custom gates could grow the register's amplitudes past 2^100 (the running
+    // product of their effective maps' Frobenius norms times the register's bound) runs with
+    // native f64 arithmetic instead of overflowing.
+    if (h->precision == QGPU_C128 && h->mode == QGPU_MODE_FAST && !plan.customs.empty()) {
+        double running = 1.0, peak = 1.0;
+        for (const LocalGate& g : plan.customs) {
+            running *= custom_growth(g);
+            peak = std::max(peak, running);
+        }
+        if (peak > 1.0 && !h->norm_valid) {
+            double2 r;
+            st = reduce_state(h, 0, &r);
+            if (st != QGPU_OK) return st;
+            h->norm_bound = std::sqrt(std::max(0.0, r.x)) * (1.0 + 1e-9);
+            h->norm_valid = true;
+        }
+        if (h->norm_bound * peak > 0x1p100) {
+            h->mode = QGPU_MODE_F64;
+            Plan wide;
+            st = build_plan(ops, n_ops, h->n_qubits, mats, n_mat_doubles, none_flags, n_none_flags,
+                            plan_options_for(h), &wide);
+            if (st == QGPU_OK) st = run_plan(h, wide, true);
+            h->mode = QGPU_MODE_FAST;
+            return st;
+        }
+    }
     // queued without a final synchronisation unless the plan can report a bounded-wait timeout
     return run_plan(h, plan, pipe_enabled() != 0 || pair2_tc_enabled());
 }

@@ -544,3 +544,27 @@ def test_measure_all_without_cache_stochastic_custom_redraws():
     assert sum(bins.values()) == shots
     sd = math.sqrt(shots * p * (1 - p))
     assert abs(ones - shots * p) < 6 * sd + 1
+
+
+def test_fast_mode_keeps_range_of_growing_custom_blocks(oracle):
+    """Custom gates that scale a wire by 2^60, applied twice (amplitudes up to ~2^120): beyond the
+    float pairs' exponent range, so the fast mode runs the program with native f64 arithmetic
+    (the plan's growth bound) and stays within 1e-12 relative of the oracle instead of
+    overflowing."""
+    n = 9
+    b = ProgramBuilder(n)
+    for w in range(n):
+        b.add("H", w)
+        b.add("Ry", w, (), param=0.1 * (w + 1))
+    big = np.array([[2.0 ** 60, 0], [0, 2.0 ** 60]], np.complex128)
+    b.add_custom(3, [], big, np.zeros(2, np.uint8))
+    b.add("CNot", 4, (3,))
+    b.add_custom(5, [], big, np.zeros(2, np.uint8))
+    for w in range(n):
+        b.add("Rz", w, (), param=0.2 * w)
+    prog = b.build()
+    ref = oracle.simulate(prog, engine=oracle.DENSE)
+    out = run_gpu(prog, "fast")
+    assert np.all(np.isfinite(out))
+    assert np.max(np.abs(out - ref)) <= 1e-12 * np.max(np.abs(ref))
+
