@@ -148,18 +148,16 @@ __host__ __device__ __forceinline__ void chain(const float d[NW], const int32_t 
     t[7] = kap[8] + (t[6] >> 7);
 }
 
-// The MMAs of one chunk (16 output reals): digit i of A times matrix digits j in [jmin, jend)
-// into the weights i + j, all accumulating onto the MAGIC_F seed. Every pair with i + j >= WMIN
-// appears once (49 pairs). (`init` marks the first step touching each weight; unused since the
-// seed MMA initialises every weight.)
+// The MMAs of one block: digit i of A times matrix digits j in [jmin, jend) into the weights
+// i + j (N = 32 (jend - jmin) output columns), all accumulating onto the MAGIC_F seed. Every
+// pair with i + j >= WMIN appears once (49 pairs), and each digit of A is read by one step.
 struct MmaStep {
-    int i, jmin, jend, init;
+    int i, jmin, jend;
 };
-constexpr int NSTEPS = 10;
+constexpr int NSTEPS = 8;
 __host__ __device__ __forceinline__ MmaStep mma_step(int s) {
-    const MmaStep tab[NSTEPS] = {{5, 0, 8, 1}, {6, 0, 7, 0}, {6, 7, 8, 1}, {7, 0, 7, 0},
-                                 {7, 7, 8, 1}, {4, 1, 8, 0}, {3, 2, 8, 0}, {2, 3, 8, 0},
-                                 {1, 4, 8, 0}, {0, 5, 8, 0}};
+    const MmaStep tab[NSTEPS] = {{5, 0, 8}, {6, 0, 8}, {7, 0, 8}, {4, 1, 8},
+                                 {3, 2, 8}, {2, 3, 8}, {1, 4, 8}, {0, 5, 8}};
     return tab[s];
 }
 
