@@ -8,7 +8,8 @@
 // vectors before the gate is undone; Phase(theta) = exp(i theta / 2) I gives -Im <lambda|phi>.
 // Then phi <- U_l^dagger phi and lambda <- U_l^dagger lambda. In QGPU_MODE_FAST the runs of
 // single-wire gates go through k_adj_tile (all gates of a wire, or of two wires, per pass, float-
-// pair arithmetic); QGPU_MODE_F64 uses k_adj_1q, one gate per pass in f64. Multi-wire gates are
+// pair arithmetic), or up to 22 qubits k_adj_group (the wires of a tile of up to 11 bits per
+// pass); QGPU_MODE_F64 uses k_adj_1q, one gate per pass in f64. Multi-wire gates are
 // undone with the fused gate passes of program.cu on each vector.
 #include <algorithm>
 #include <array>
@@ -341,15 +342,225 @@ k_adj_tile(double2* __restrict__ phi, double2* __restrict__ lam,
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// k_adj_group: the runs of single-wire gates of the reverse sweep on up to ADJ_GROUP_MAX_BITS
+// wires in one pass over phi and lambda (in place, resident float-pair layout). A CTA stages a
+// tile of both vectors in shared memory: the 2^K amplitudes that share every bit outside the
+// pass's K tile bits (the wires' bits and the lowest other bits, so that 32 consecutive
+// amplitudes load together). Then, wire by wire, each thread takes the wire's Pauli sums over its
+// pairs (packed Dot2, reduced per warp in float pairs into shared accumulators) and applies the
+// run's undo to its pairs of both vectors. Gates on different wires commute and a wire's sums are
+// taken before its own undo, so the results are those of one pass per wire (k_adj_tile with
+// Pauli steps), with one read and one write of each vector per pass.
+// ---------------------------------------------------------------------------------------------
+constexpr int ADJ_GROUP_MAX_BITS = 11;
+constexpr int ADJ_GROUP_THREADS = 256;
+constexpr int ADJ_GROUP_WARPS = ADJ_GROUP_THREADS / 32;
+
+struct AdjGroupWire {
+    int lb;      // tile bit of the wire
+    int row[4];  // partial rows of its sums over X, Y, Z, -I (-1: not needed)
+    u64 pk[32];  // ST_DENSE packed constants of the run's undo
+};
+struct AdjGroupParams {
+    uint64_t ngroups;
+    int nbits;
+    int bits[ADJ_GROUP_MAX_BITS];  // ascending
+    int nwires;
+    int nb;                        // row length of partial (>= the grid)
+    AdjGroupWire w[ADJ_GROUP_MAX_BITS];
+};
+
+__host__ __device__ constexpr size_t adj_group_smem(int nbits) {
+    return (size_t)2 * 16 * ((size_t)1 << nbits) + (size_t)ADJ_GROUP_WARPS * ADJ_GROUP_MAX_BITS * 4 * 8 +
+           (32 + 64) * 8;
+}
+
+// (h, l) += (bh, bl) in float-pair arithmetic (TwoSum of the heads, then the tails)
+__device__ __forceinline__ void ff2_acc(float& h, float& l, float bh, float bl) {
+    const float s = __fadd_rn(h, bh);
+    const float bb = __fadd_rn(s, -h);
+    float e = __fadd_rn(__fadd_rn(h, -__fadd_rn(s, -bb)), __fadd_rn(bh, -bb));
+    e = __fadd_rn(e, __fadd_rn(l, bl));
+    h = __fadd_rn(s, e);
+    l = __fadd_rn(e, -__fadd_rn(h, -s));
+}
+
+__global__ void __launch_bounds__(ADJ_GROUP_THREADS, 2)
+k_adj_group(double2* __restrict__ phi, double2* __restrict__ lam,
+            const __grid_constant__ AdjGroupParams p, double* __restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int T = 1 << p.nbits;
+    double2* sf = reinterpret_cast<double2*>(smem);    // phi tile
+    double2* sl = sf + T;                               // lambda tile
+    float2* sacc = reinterpret_cast<float2*>(sl + T);   // [warp][wire][pauli] float pairs
+    uint64_t* lo_tab = reinterpret_cast<uint64_t*>(sacc + ADJ_GROUP_WARPS * ADJ_GROUP_MAX_BITS * 4);
+    uint64_t* hi_tab = lo_tab + 32;                     // [T >> nlo] (at most 64)
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nlo = p.nbits < 5 ? p.nbits : 5;
+    for (int i = tid; i < 32 + (T >> nlo); i += ADJ_GROUP_THREADS) {
+        uint64_t o = 0;
+        if (i < 32) {
+            for (int m = 0; m < nlo; ++m)
+                if ((i >> m) & 1) o |= 1ull << p.bits[m];
+            lo_tab[i] = o;
+        } else {
+            const int v = i - 32;
+            for (int m = nlo; m < p.nbits; ++m)
+                if ((v >> (m - nlo)) & 1) o |= 1ull << p.bits[m];
+            hi_tab[v] = o;
+        }
+    }
+    for (int i = tid; i < ADJ_GROUP_WARPS * ADJ_GROUP_MAX_BITS * 4; i += ADJ_GROUP_THREADS)
+        sacc[i] = make_float2(0.f, 0.f);
+    __syncthreads();
+    const int lomask = (1 << nlo) - 1;
+    for (uint64_t g = blockIdx.x; g < p.ngroups; g += gridDim.x) {
+        uint64_t base = g;
+        for (int m = 0; m < p.nbits; ++m) base = insert_zero(base, p.bits[m]);
+        for (int i = tid; i < T; i += ADJ_GROUP_THREADS) {
+            const uint64_t o = base | lo_tab[i & lomask] | hi_tab[i >> nlo];
+            sf[i] = phi[o];
+            sl[i] = lam[o];
+        }
+        __syncthreads();
+        for (int w = 0; w < p.nwires; ++w) {
+            const int lb = p.w[w].lb;
+            const u64* pk = p.w[w].pk;
+            PDot2 acc[4];
+            bool first[4] = {true, true, true, true};
+            const bool need[4] = {p.w[w].row[0] >= 0, p.w[w].row[1] >= 0, p.w[w].row[2] >= 0,
+                                  p.w[w].row[3] >= 0};
+            for (int q = tid; q < (T >> 1); q += ADJ_GROUP_THREADS) {
+                const int i0 = ((q >> lb) << (lb + 1)) | (q & ((1 << lb) - 1));
+                const int i1 = i0 | (1 << lb);
+                ffp f0 = ffr_load(sf[i0]), f1 = ffr_load(sf[i1]);
+                ffp l0 = ffr_load(sl[i0]), l1 = ffr_load(sl[i1]);
+                ffp f0s, f1s;  // swapped lanes (im, re)
+                f0s.h = pswap(f0.h);
+                f0s.l = pswap(f0.l);
+                f1s.h = pswap(f1.h);
+                f1s.l = pswap(f1.l);
+                if (need[0]) {  // X: Im(l0* f1) + Im(l1* f0)
+                    adj_term(acc[0], first[0], l0, f1s, 1.f, -1.f);
+                    adj_term(acc[0], first[0], l1, f0s, 1.f, -1.f);
+                }
+                if (need[1]) {  // Y: -Re(l0* f1) + Re(l1* f0)
+                    adj_term(acc[1], first[1], l0, f1, -1.f, -1.f);
+                    adj_term(acc[1], first[1], l1, f0, 1.f, 1.f);
+                }
+                if (need[2]) {  // Z: Im(l0* f0) - Im(l1* f1)
+                    adj_term(acc[2], first[2], l0, f0s, 1.f, -1.f);
+                    adj_term(acc[2], first[2], l1, f1s, -1.f, 1.f);
+                }
+                if (need[3]) {  // global phase: -(Im(l0* f0) + Im(l1* f1))
+                    adj_term(acc[3], first[3], l0, f0s, -1.f, 1.f);
+                    adj_term(acc[3], first[3], l1, f1s, -1.f, 1.f);
+                }
+                ff_dense(f0, f1, pk);
+                ff_dense(l0, l1, pk);
+                sf[i0] = ffr_store(f0);
+                sf[i1] = ffr_store(f1);
+                sl[i0] = ffr_store(l0);
+                sl[i1] = ffr_store(l1);
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (!need[m]) continue;
+                float h = 0.f, l = 0.f;
+                if (!first[m]) {
+                    u64 rh, rl;
+                    acc[m].result(rh, rl);
+                    float h1, l1;
+                    up2(rh, h, h1);
+                    up2(rl, l, l1);
+                    ff2_acc(h, l, h1, l1);
+                }
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) {
+                    const float oh = __shfl_down_sync(0xffffffffu, h, d);
+                    const float ol = __shfl_down_sync(0xffffffffu, l, d);
+                    ff2_acc(h, l, oh, ol);
+                }
+                if (lane == 0) {
+                    float2& a = sacc[(warp * ADJ_GROUP_MAX_BITS + w) * 4 + m];
+                    ff2_acc(a.x, a.y, h, l);
+                }
+            }
+            __syncthreads();
+        }
+        for (int i = tid; i < T; i += ADJ_GROUP_THREADS) {
+            const uint64_t o = base | lo_tab[i & lomask] | hi_tab[i >> nlo];
+            phi[o] = sf[i];
+            lam[o] = sl[i];
+        }
+        __syncthreads();
+    }
+    // per-CTA sums into column blockIdx.x; columns past the grid (partial rows have nb columns) get 0
+    for (int k = tid; k < p.nwires * 4; k += ADJ_GROUP_THREADS) {
+        const int w = k >> 2, m = k & 3;
+        if (p.w[w].row[m] < 0) continue;
+        double t = 0.0;
+        for (int v = 0; v < ADJ_GROUP_WARPS; ++v) {
+            const float2 a = sacc[(v * ADJ_GROUP_MAX_BITS + w) * 4 + m];
+            t += (double)a.x + (double)a.y;
+        }
+        double* row = partial + (size_t)p.w[w].row[m] * p.nb;
+        row[blockIdx.x] = t;
+        for (int c = blockIdx.x + gridDim.x; c < p.nb; c += gridDim.x) row[c] = 0.0;
+    }
+}
+
+// Event-timed launch under qgpu_set_profiling (filed under `name`, bytes = reads + writes of both
+// vectors); a plain launch otherwise.
+template <class F>
+static int adj_profiled(qgpu_handle* h, const char* name, double bytes, F&& launch) {
+    size_t base = 0;
+    if (h->profile) {
+        int st = prof_events(h, 1, &base);
+        if (st != QGPU_OK) return st;
+        QGPU_CUDA(cudaEventRecord(h->events[2 * base], h->stream));
+    }
+    int st = launch();
+    if (st != QGPU_OK) return st;
+    if (h->profile) {
+        QGPU_CUDA(cudaEventRecord(h->events[2 * base + 1], h->stream));
+        return prof_collect(h, {name}, {bytes});
+    }
+    return QGPU_OK;
+}
+
+static int launch_adj_group(qgpu_handle* h, double2* phi, double2* lam, const AdjGroupParams& p,
+                            double* partial) {
+    const size_t smem = adj_group_smem(p.nbits);
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        k_adj_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_group_smem(ADJ_GROUP_MAX_BITS));
+    QGPU_CUDA(attr);
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adj_group, ADJ_GROUP_THREADS, smem) != cudaSuccess || occ < 1)
+        occ = 1;
+    const uint64_t grid = std::max<uint64_t>(
+        1, std::min<uint64_t>({p.ngroups, (uint64_t)h->sm_count * occ, (uint64_t)p.nb}));
+    return adj_profiled(h, "k_adj_group", 64.0 * (double)h->dim, [&]() -> int {
+        k_adj_group<<<(unsigned)grid, ADJ_GROUP_THREADS, smem, h->stream>>>(phi, lam, p, partial);
+        QGPU_CHECK_LAUNCH("k_adj_group");
+        h->launches++;
+        h->h2d_bytes += sizeof(p);
+        return QGPU_OK;
+    });
+}
+
 template <int K>
 static int launch_adj_tile(qgpu_handle* h, double2* phi, double2* lam, const AdjTileParams& p,
                            double* partial) {
     // phi and lambda stay in the resident float-pair layout for the whole sweep
-    k_adj_tile<K, true><<<p.nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, p, partial);
-    QGPU_CHECK_LAUNCH("k_adj_tile");
-    h->launches++;
-    h->h2d_bytes += sizeof(AdjTileParams);
-    return QGPU_OK;
+    return adj_profiled(h, "k_adj_tile", 64.0 * (double)h->dim, [&]() -> int {
+        k_adj_tile<K, true><<<p.nb, ADJ_THREADS, 0, h->stream>>>(phi, lam, p, partial);
+        QGPU_CHECK_LAUNCH("k_adj_tile");
+        h->launches++;
+        h->h2d_bytes += sizeof(AdjTileParams);
+        return QGPU_OK;
+    });
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -566,7 +777,64 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
         // 24 qubits: 35.1 against 29.9 ms). Tuning knob QGPU_ADJ_PAULI: 0 / 1 forces either.
         const char* pk = std::getenv("QGPU_ADJ_PAULI");  // read per call (tests force either)
         const int pauli_knob = (pk && pk[0] == '0') ? 0 : (pk && pk[0] == '1') ? 1 : -1;
+        // Grouped passes (k_adj_group: the wires of a run in tiles of up to 11 bits, one pass
+        // per tile) up to 22 qubits; QGPU_ADJ_GROUP=0 / 1 (read per call) forces them off / on.
+        // Measured on GB300 (4-layer ansatz, energy + gradient): 20 qubits 5.23 against 6.34 ms
+        // (30 launches instead of 200), 22 qubits 7.72 against 7.76 ms, 24 qubits 31.8 against
+        // 29.8 ms: a wire's float-pair sums and undo keep the FMA pipe 64 % busy for about as
+        // long as one streaming pass over both vectors takes, so from 23 qubits the per-wire
+        // passes (HBM-bound, the arithmetic hidden under the traffic) are kept.
+        const char* gk = std::getenv("QGPU_ADJ_GROUP");
+        const bool group = pauli_knob != 0 && (gk ? gk[0] != '0' : h->n_qubits <= 22);
         const bool pauli = pauli_knob >= 0 ? pauli_knob == 1 : h->n_qubits >= 22;
+        if (group) {
+            std::vector<PauliRun> prs(wires.size());
+            for (size_t w = 0; w < wires.size(); ++w) {
+                int s3 = pauli_run(ops, gates[w], h->n_qubits, &prs[w]);
+                if (s3 != QGPU_OK) return s3;
+            }
+            std::vector<size_t> order(wires.size());
+            for (size_t w = 0; w < order.size(); ++w) order[w] = w;
+            std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return wires[x] < wires[y]; });
+            const int kmax = std::min(h->n_qubits, ADJ_GROUP_MAX_BITS);
+            const uint64_t low = (1ull << std::min(h->n_qubits, 5)) - 1;  // coalescing: bits 0..4 in every tile
+            size_t i = 0;
+            while (i < order.size()) {
+                uint64_t mask = low;
+                std::vector<size_t> chosen;
+                while (i < order.size() && __builtin_popcountll(mask | (1ull << wires[order[i]])) <= kmax) {
+                    mask |= 1ull << wires[order[i]];
+                    chosen.push_back(order[i++]);
+                }
+                for (int b = 0; b < h->n_qubits && __builtin_popcountll(mask) < kmax; ++b) mask |= 1ull << b;
+                AdjGroupParams p;
+                std::memset(&p, 0, sizeof(p));
+                for (int b = 0; b < 64; ++b)
+                    if ((mask >> b) & 1ull) p.bits[p.nbits++] = b;
+                p.ngroups = h->dim >> p.nbits;
+                p.nb = nb;
+                p.nwires = (int)chosen.size();
+                for (int c = 0; c < p.nwires; ++c) {
+                    const size_t w = chosen[c];
+                    AdjGroupWire& gw = p.w[c];
+                    gw.lb = (int)(std::find(p.bits, p.bits + p.nbits, wires[w]) - p.bits);
+                    int kind_row[5] = {-1, -1, -1, -1, -1};
+                    for (int m = 1; m <= 4; ++m) {
+                        gw.row[m - 1] = -1;
+                        if (prs[w].need[m]) gw.row[m - 1] = kind_row[m] = nrows++;
+                    }
+                    const std::array<cd, 4>& undo = prs[w].undo;
+                    const DevStep ds = dense_step(undo[0], undo[1], undo[2], undo[3]);
+                    std::memcpy(gw.pk, ds.pk, sizeof(gw.pk));
+                    for (const auto& r : prs[w].rots)
+                        for (int m = 1; m <= 4; ++m)
+                            if (r.second[m] != 0.0) terms[r.first].emplace_back(kind_row[m], r.second[m]);
+                }
+                int s2 = launch_adj_group(h, phi, lam, p, partial);
+                if (s2 != QGPU_OK) return s2;
+            }
+            return QGPU_OK;
+        }
         if (tile_bits == 1 && pauli) {
             // One pass per wire: the sums <lambda| s |phi> for the Paulis s the run's rotations
             // need, all taken before any of its gates is undone, then the whole run undone as one

@@ -48,11 +48,18 @@ def test_energy_matches_oracle(oracle):
     assert e == pytest.approx(_oracle_energy(oracle, prog, an.a, an.b), abs=1e-12)
 
 
-@pytest.fixture(params=["gates", "pauli"])
+@pytest.fixture(params=["gates", "pauli", "group"])
 def sweep(request, monkeypatch):
-    """Both single-wire sweep forms: per-gate passes, and one pass per wire with the gradients
-    formed from Pauli sums (the default from 22 qubits on)."""
-    monkeypatch.setenv("QGPU_ADJ_PAULI", "1" if request.param == "pauli" else "0")
+    """The single-wire sweep forms: per-gate passes; one pass per wire with the gradients formed
+    from Pauli sums; the same sums for the wires of a tile of up to 11 bits in one pass (the
+    default)."""
+    if request.param == "gates":
+        monkeypatch.setenv("QGPU_ADJ_PAULI", "0")
+    elif request.param == "pauli":
+        monkeypatch.setenv("QGPU_ADJ_PAULI", "1")
+        monkeypatch.setenv("QGPU_ADJ_GROUP", "0")
+    else:
+        monkeypatch.setenv("QGPU_ADJ_GROUP", "1")
     return request.param
 
 
@@ -163,6 +170,29 @@ def test_adjoint_ansatz_20q_vs_fd_and_parameter_shift():
     assert np.max(np.abs(g - fd)) <= 1e-7
     assert np.max(np.abs(g - ps)) <= 1e-9
     assert math.isfinite(e)
+
+
+@pytest.mark.parametrize("n,layers", [(16, 3), (23, 2)])
+def test_grouped_sweep_equals_per_wire_passes(monkeypatch, n, layers):
+    """k_adj_group (the wires of a tile of up to 11 bits per pass: at 23 qubits tiles of bits
+    0..10, then bits 0..4 with six more wires, twice) against one pass per wire: the same
+    Pauli sums in another summation order, so energies equal and gradients within 1e-11."""
+    an = W.ansatz(n=n, layers=layers, seed=12)
+    prog = an.program()
+    h = nat.Handle(n)
+    h.set_profiling(True)
+    monkeypatch.setenv("QGPU_ADJ_GROUP", "1")
+    e1, g1 = GR.energy_and_gradient(h, prog, an.a, an.b)
+    prof = h.profile(reset=True)
+    assert prof["k_adj_group"][0] == layers * (1 if n <= 11 else 1 + -(-(n - 11) // 6)), prof
+    monkeypatch.setenv("QGPU_ADJ_GROUP", "0")
+    monkeypatch.setenv("QGPU_ADJ_PAULI", "1")
+    e2, g2 = GR.energy_and_gradient(h, prog, an.a, an.b)
+    prof2 = h.profile(reset=True)
+    assert "k_adj_group" not in prof2 and prof2["k_adj_tile"][0] == layers * n
+    h.close()
+    assert e1 == e2
+    assert np.max(np.abs(g1 - g2)) <= 1e-11
 
 
 def test_adjoint_rejects_custom():
