@@ -311,7 +311,8 @@ def run_batch_leg(args) -> None:
     4 layers each, own angles and observables; energies + adjoint gradients for every circuit in
     one qgpu_batch_run call per rank. Under torchrun the circuits shard across ranks by cost
     (batch.shard) and the results come back with one all-reduce of flat arrays; the time is the
-    slowest rank's, between barriers. Reports circuits/s and the fusion budget tuned per size."""
+    slowest rank's, between barriers. Reports circuits/s and, per size, the fusion budget and
+    adjoint sweep form the autotuner picked."""
     import torch
 
     from quantr_gb300 import _native as nat
@@ -353,7 +354,7 @@ def run_batch_leg(args) -> None:
             torch.distributed.all_reduce(dt, op=torch.distributed.ReduceOp.MAX)
         dt = float(dt.item())
         out["results"][pname] = {"seconds": dt, "circuits_per_s": len(cs) / dt,
-                                 "tuned_ff_budget_per_qubits": tuned,
+                                 "tuned_per_qubits": tuned,
                                  "small_circuits_in_shared_memory": sum(
                                      1 for c in cs if c.n <= (12 if pname == "c128" else 13))}
         if pname == "c128" and rank == 0:

@@ -208,8 +208,10 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
  * energies[i] and d energy / d angle for every op (grads[grad_offset + g]). Circuits small
  * enough for shared memory (complex128 <= 12 qubits, complex64 <= 13) run in one persistent
  * launch replayed from a CUDA graph; larger ones run through the register-tile passes with a
- * per-size fusion budget picked by timing (written to tuned_budget[n_qubits] when not NULL,
- * an int[41]), in complex128 whatever `precision` says (the adjoint sweep is complex128 only).
+ * per-size fusion budget and adjoint sweep form picked by timing (written to
+ * tuned_budget[n_qubits] when not NULL, an int[41]: the budget, plus 65536 when the sweep takes
+ * the single-wire gates of up to 11 wires per pass rather than one pass per wire), in complex128
+ * whatever `precision` says (the adjoint sweep is complex128 only).
  * Custom gates are rejected (QGPU_ERR_NONUNITARY). */
 typedef struct qgpu_batch_item {
     int32_t n_qubits;

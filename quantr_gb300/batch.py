@@ -58,7 +58,8 @@ def batch_config(count: int = 4096, seed: int = 5, layers: int = 4, n_min: int =
 
 
 def run_batch(circuits: list[BatchCircuit], precision: int = nat.QGPU_C128):
-    """Energies [len] and per-circuit gradient arrays (one entry per op) on the current GPU."""
+    """Energies [len], per-circuit gradient arrays (one entry per op) and, per qubit count of
+    the register-pass circuits, the autotuner's picks, all on the current GPU."""
     lib = nat.lib()
     items = (QgpuBatchItem * max(1, len(circuits)))()
     ops, obs = [], []
@@ -89,8 +90,11 @@ def run_batch(circuits: list[BatchCircuit], precision: int = nat.QGPU_C128):
     out_g = []
     for i, c in enumerate(circuits):
         out_g.append(grads[items[i].grad_offset: items[i].grad_offset + len(c.program.ops)].copy())
-    budgets = {q: tuned[q] for q in range(41) if tuned[q]}
-    return energies, out_g, budgets
+    # per size: the float-pair fusion budget and the adjoint sweep form the autotuner picked
+    picks = {q: {"ff_budget": tuned[q] & 0xFFFF,
+                 "adjoint_sweep": "grouped" if tuned[q] >> 16 else "per-wire"}
+             for q in range(41) if tuned[q]}
+    return energies, out_g, picks
 
 
 def shard(circuits: list, world: int) -> list[list[int]]:

@@ -784,8 +784,10 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
         // 29.8 ms: a wire's float-pair sums and undo keep the FMA pipe 64 % busy for about as
         // long as one streaming pass over both vectors takes, so from 23 qubits the per-wire
         // passes (HBM-bound, the arithmetic hidden under the traffic) are kept.
+        // The batch autotuner's pick (h->adj_group) comes first.
         const char* gk = std::getenv("QGPU_ADJ_GROUP");
-        const bool group = pauli_knob != 0 && (gk ? gk[0] != '0' : h->n_qubits <= 22);
+        const int forced = h->adj_group >= 0 ? h->adj_group : gk ? (gk[0] != '0' ? 1 : 0) : -1;
+        const bool group = pauli_knob != 0 && (forced >= 0 ? forced == 1 : h->n_qubits <= 22);
         const bool pauli = pauli_knob >= 0 ? pauli_knob == 1 : h->n_qubits >= 22;
         if (group) {
             std::vector<PauliRun> prs(wires.size());

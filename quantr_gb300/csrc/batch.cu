@@ -338,14 +338,16 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
 #undef BATCH_TRY
     }
     // ---- large circuits: register-tile passes. The fusion budget is tuned once per size (the
-    // forward pass timed per candidate); then W host threads, each with its own handles (and so
+    // forward pass timed per candidate), and so is the adjoint sweep's width (one energy +
+    // gradient timed with the runs of single-wire gates grouped in tiles of up to 11 wires per
+    // pass, and with one pass per wire); then W host threads, each with its own handles (and so
     // its own stream), take circuits largest first from a shared counter, so that the launch and
     // synchronisation overhead of medium circuits overlaps with other circuits' kernels.
     if (large.empty()) return QGPU_OK;
     std::stable_sort(large.begin(), large.end(), [&](size_t x, size_t y) {
         return items[x].n_qubits > items[y].n_qubits;
     });
-    std::map<int, int> budget;
+    std::map<int, int> budget, sweep;
     {
         std::map<int, qgpu_handle*> tune;
         int st = QGPU_OK;
@@ -374,7 +376,22 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
             }
             if (st != QGPU_OK) break;
             budget[it.n_qubits] = pick;
-            if (tuned_budget) tuned_budget[it.n_qubits] = pick;
+            h->batch_budget = pick;
+            // the sweep form: a first (untimed) gradient allocates the work vectors
+            std::vector<double> g((size_t)std::max(1, it.n_ops));
+            double e = 0.0, tsweep[2] = {0.0, 0.0};
+            for (int form : {1, 1, 0}) {
+                h->adj_group = form;
+                qgpu_set_zero(h);
+                auto t0 = std::chrono::steady_clock::now();
+                st = qgpu_adjoint_grad(h, po, (size_t)it.n_ops, nullptr, 0, nullptr, 0, obs + it.obs_offset,
+                                       obs + it.obs_offset + it.n_qubits, &e, g.data());
+                if (st != QGPU_OK) break;
+                tsweep[form] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            }
+            if (st != QGPU_OK) break;
+            sweep[it.n_qubits] = tsweep[1] <= tsweep[0] ? 1 : 0;
+            if (tuned_budget) tuned_budget[it.n_qubits] = pick + (sweep[it.n_qubits] ? 65536 : 0);
         }
         for (auto& kv : tune) qgpu_destroy(kv.second);
         if (st != QGPU_OK) return st;
@@ -398,6 +415,7 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
             if (!h) st = qgpu_create(it.n_qubits, QGPU_C128, &h);
             if (st == QGPU_OK) {
                 h->batch_budget = budget[it.n_qubits];
+                h->adj_group = sweep[it.n_qubits];
                 st = qgpu_set_zero(h);
             }
             if (st == QGPU_OK)

@@ -49,6 +49,8 @@ struct qgpu_handle {
     int block_qubits = 0;      // > 0: fuse gates into dense blocks of this many wires
     int block_gates = 12;      // at most this many gates per dense block
     int batch_budget = 0;      // > 0: float-pair fusion budget picked by the batch autotuner
+    int adj_group = -1;        // adjoint sweep form picked by the batch autotuner: 1 grouped
+                               // tiles (k_adj_group), 0 per-wire passes, -1 by size
     int device = 0;
     int sm_count = 0;
     uint64_t dim = 0;          // 2^n amplitudes

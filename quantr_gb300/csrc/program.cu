@@ -931,7 +931,10 @@ __global__ void __launch_bounds__(256) k_xor_perm(S* __restrict__ st, uint64_t d
 // lowest bits and their images (|B| <= 10, closed under pi); a tile = the 2^|B| amplitudes that
 // share all other bits (a base). pi maps tile(base) onto tile(pi(base)): a CTA owns both tiles of
 // a pair (or one tile that maps onto itself), stages them in shared memory with coalesced loads
-// (low bits fastest) and writes each destination tile with coalesced stores, in place.
+// (low bits fastest) and writes each destination tile with coalesced stores, in place. Tile slot
+// l sits at l ^ ((l >> 5) & 31) in shared memory: the loads (32 consecutive l per warp) and the
+// gather of a bit reversal (which sends the lane bits to the tile's high bits) both touch every
+// bank group equally instead of the gather hitting one.
 // ---------------------------------------------------------------------------------------------
 constexpr int BP_MAX_BITS = 10;
 
@@ -942,6 +945,8 @@ struct BitPermArgs {
     int n;
     uint64_t nbases;           // 2^(n - nb)
 };
+
+__device__ __forceinline__ int bp_swz(int l) { return l ^ ((l >> 5) & 31); }
 
 template <class S>
 __global__ void __launch_bounds__(256) k_bitperm(S* __restrict__ st, const __grid_constant__ BitPermArgs p) {
@@ -974,14 +979,15 @@ __global__ void __launch_bounds__(256) k_bitperm(S* __restrict__ st, const __gri
         if (pbase < base) continue;  // the partner tile's CTA moves this pair
         const bool self = pbase == base;
         for (int l = threadIdx.x; l < T; l += blockDim.x) {
-            tA[l] = st[base | offB[l]];
-            if (!self) tB[l] = st[pbase | offB[l]];
+            tA[bp_swz(l)] = st[base | offB[l]];
+            if (!self) tB[bp_swz(l)] = st[pbase | offB[l]];
         }
         __syncthreads();
         // destination d = base | spread(l) receives pi(d) = pbase | spread(pl[l])
         for (int l = threadIdx.x; l < T; l += blockDim.x) {
-            st[base | offB[l]] = self ? tA[pl[l]] : tB[pl[l]];
-            if (!self) st[pbase | offB[l]] = tA[pl[l]];
+            const int q = bp_swz(pl[l]);
+            st[base | offB[l]] = self ? tA[q] : tB[q];
+            if (!self) st[pbase | offB[l]] = tA[q];
         }
         __syncthreads();
     }

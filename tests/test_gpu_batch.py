@@ -41,6 +41,7 @@ def test_batch_c128_matches_per_circuit():
     for a, b in zip(g, rg):
         assert np.max(np.abs(a - b)) <= 1e-10
     assert tuned and all(q > 12 for q in tuned)
+    assert all(t["adjoint_sweep"] in ("grouped", "per-wire") and t["ff_budget"] > 0 for t in tuned.values())
 
 
 def test_batch_c64_energies_and_gradients():
