@@ -187,7 +187,8 @@ int qgpu_compare(qgpu_handle* a, qgpu_handle* b, double* max_abs_diff, double* i
 
 /* ---- differentiation (no counterpart in quantr) ------------------------------------------
  * Observable H = sum_i a[i] Z_i Z_{(i+1) mod n} + sum_i b[i] X_i over the n wires (periodic),
- * a and b of length n. complex128 handles only. */
+ * a and b of length n. complex128 handles compute in f64 / float pairs; complex64 handles in f32
+ * (the sums over the register in f64), gradients within about 1e-5 of the complex128 ones. */
 
 /* <psi|H|psi> of the current register. */
 int qgpu_expectation_zzx(qgpu_handle* h, const double* a, const double* b, double* energy);
@@ -210,8 +211,8 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops,
  * launch replayed from a CUDA graph; larger ones run through the register-tile passes with a
  * per-size fusion budget and adjoint sweep form picked by timing (written to
  * tuned_budget[n_qubits] when not NULL, an int[41]: the budget, plus 65536 when the sweep takes
- * the single-wire gates of up to 11 wires per pass rather than one pass per wire), in complex128
- * whatever `precision` says (the adjoint sweep is complex128 only).
+ * the single-wire gates of up to 11 wires per pass rather than one pass per wire; complex64
+ * sweeps always do), in the batch's precision.
  * Custom gates are rejected (QGPU_ERR_NONUNITARY). */
 typedef struct qgpu_batch_item {
     int32_t n_qubits;

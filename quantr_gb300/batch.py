@@ -90,8 +90,9 @@ def run_batch(circuits: list[BatchCircuit], precision: int = nat.QGPU_C128):
     out_g = []
     for i, c in enumerate(circuits):
         out_g.append(grads[items[i].grad_offset: items[i].grad_offset + len(c.program.ops)].copy())
-    # per size: the float-pair fusion budget and the adjoint sweep form the autotuner picked
-    picks = {q: {"ff_budget": tuned[q] & 0xFFFF,
+    # per size: the fusion budget (float-pair for complex128, f32 for complex64) and the adjoint
+    # sweep form the autotuner picked
+    picks = {q: {"fusion_budget": tuned[q] & 0xFFFF,
                  "adjoint_sweep": "grouped" if tuned[q] >> 16 else "per-wire"}
              for q in range(41) if tuned[q]}
     return energies, out_g, picks

@@ -38,30 +38,36 @@ struct Ham {
     double b[MAX_HAM_QUBITS];
 };
 
-// lambda = H psi, and per-block partial sums of Re(conj(psi) lambda)
+// lambda = H psi, and per-block partial sums of Re(conj(psi) lambda). T = double2 (complex128,
+// f64 arithmetic) or float2 (complex64: lambda in f32, the energy sums in f64).
+template <class T>
 __global__ void __launch_bounds__(ADJ_THREADS)
-k_apply_zzx(const double2* __restrict__ psi, double2* __restrict__ lam, uint64_t dim,
+k_apply_zzx(const T* __restrict__ psi, T* __restrict__ lam, uint64_t dim,
             const __grid_constant__ Ham H, double* __restrict__ partial) {
+    using R = decltype(T::x);
     __shared__ double sh[ADJ_THREADS];
     double acc = 0.0;
     const int n = H.n;
     for (uint64_t x = blockIdx.x * (uint64_t)ADJ_THREADS + threadIdx.x; x < dim;
          x += (uint64_t)gridDim.x * ADJ_THREADS) {
-        double d = 0.0;
+        R d = 0;
         for (int i = 0; i < n; ++i) {
             const int j = (i + 1) % n;
             const uint64_t p = ((x >> (n - 1 - i)) ^ (x >> (n - 1 - j))) & 1ull;
-            d += p ? -H.a[i] : H.a[i];
+            d += p ? -(R)H.a[i] : (R)H.a[i];
         }
-        const double2 v = psi[x];
-        double re = d * v.x, im = d * v.y;
+        const T v = psi[x];
+        R re = d * v.x, im = d * v.y;
         for (int i = 0; i < n; ++i) {
-            const double2 w = psi[x ^ (1ull << (n - 1 - i))];
-            re = fma(H.b[i], w.x, re);
-            im = fma(H.b[i], w.y, im);
+            const T w = psi[x ^ (1ull << (n - 1 - i))];
+            re = fma((R)H.b[i], w.x, re);
+            im = fma((R)H.b[i], w.y, im);
         }
-        lam[x] = make_double2(re, im);
-        acc = fma(v.x, re, fma(v.y, im, acc));
+        T o;
+        o.x = re;
+        o.y = im;
+        lam[x] = o;
+        acc = fma((double)v.x, (double)re, fma((double)v.y, (double)im, acc));
     }
     sh[threadIdx.x] = acc;
     __syncthreads();
@@ -550,6 +556,163 @@ static int launch_adj_group(qgpu_handle* h, double2* phi, double2* lam, const Ad
     });
 }
 
+// k_adj_group_f32: k_adj_group for complex64 vectors. Plain f32 complex arithmetic for the Pauli
+// sums and the undo, the sums reduced per warp in f32 and accumulated per CTA in f64.
+struct AdjGroupWireF {
+    int lb;      // tile bit of the wire
+    int row[4];  // partial rows of its sums over X, Y, Z, -I (-1: not needed)
+    float u[8];  // the run's undo, row-major complex (u00, u01, u10, u11)
+};
+struct AdjGroupParamsF {
+    uint64_t ngroups;
+    int nbits;
+    int bits[ADJ_GROUP_MAX_BITS];
+    int nwires;
+    int nb;
+    AdjGroupWireF w[ADJ_GROUP_MAX_BITS];
+};
+
+__host__ __device__ constexpr size_t adj_group_f32_smem(int nbits) {
+    return (size_t)2 * 8 * ((size_t)1 << nbits) + (size_t)ADJ_GROUP_WARPS * ADJ_GROUP_MAX_BITS * 4 * 8 +
+           (32 + 64) * 8;
+}
+
+__device__ __forceinline__ float2 cmul_add(float ur, float ui, float2 a, float vr, float vi, float2 b) {
+    return make_float2(fmaf(ur, a.x, fmaf(-ui, a.y, fmaf(vr, b.x, -vi * b.y))),
+                       fmaf(ur, a.y, fmaf(ui, a.x, fmaf(vr, b.y, vi * b.x))));
+}
+
+__global__ void __launch_bounds__(ADJ_GROUP_THREADS)
+k_adj_group_f32(float2* __restrict__ phi, float2* __restrict__ lam,
+                const __grid_constant__ AdjGroupParamsF p, double* __restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int T = 1 << p.nbits;
+    float2* sf = reinterpret_cast<float2*>(smem);
+    float2* sl = sf + T;
+    double* sacc = reinterpret_cast<double*>(sl + T);   // [warp][wire][pauli]
+    uint64_t* lo_tab = reinterpret_cast<uint64_t*>(sacc + ADJ_GROUP_WARPS * ADJ_GROUP_MAX_BITS * 4);
+    uint64_t* hi_tab = lo_tab + 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nlo = p.nbits < 5 ? p.nbits : 5;
+    for (int i = tid; i < 32 + (T >> nlo); i += ADJ_GROUP_THREADS) {
+        uint64_t o = 0;
+        if (i < 32) {
+            for (int m = 0; m < nlo; ++m)
+                if ((i >> m) & 1) o |= 1ull << p.bits[m];
+            lo_tab[i] = o;
+        } else {
+            const int v = i - 32;
+            for (int m = nlo; m < p.nbits; ++m)
+                if ((v >> (m - nlo)) & 1) o |= 1ull << p.bits[m];
+            hi_tab[v] = o;
+        }
+    }
+    for (int i = tid; i < ADJ_GROUP_WARPS * ADJ_GROUP_MAX_BITS * 4; i += ADJ_GROUP_THREADS) sacc[i] = 0.0;
+    __syncthreads();
+    const int lomask = (1 << nlo) - 1;
+    for (uint64_t g = blockIdx.x; g < p.ngroups; g += gridDim.x) {
+        uint64_t base = g;
+        for (int m = 0; m < p.nbits; ++m) base = insert_zero(base, p.bits[m]);
+        for (int i = tid; i < T; i += ADJ_GROUP_THREADS) {
+            const uint64_t o = base | lo_tab[i & lomask] | hi_tab[i >> nlo];
+            sf[i] = phi[o];
+            sl[i] = lam[o];
+        }
+        __syncthreads();
+        for (int w = 0; w < p.nwires; ++w) {
+            const AdjGroupWireF& W = p.w[w];
+            const int lb = W.lb;
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int q = tid; q < (T >> 1); q += ADJ_GROUP_THREADS) {
+                const int i0 = ((q >> lb) << (lb + 1)) | (q & ((1 << lb) - 1));
+                const int i1 = i0 | (1 << lb);
+                const float2 f0 = sf[i0], f1 = sf[i1], l0 = sl[i0], l1 = sl[i1];
+                // Im(conj(a) b) = a.x b.y - a.y b.x, Re(conj(a) b) = a.x b.x + a.y b.y
+                const float i01 = fmaf(l0.x, f1.y, -l0.y * f1.x), i10 = fmaf(l1.x, f0.y, -l1.y * f0.x);
+                const float r01 = fmaf(l0.x, f1.x, l0.y * f1.y), r10 = fmaf(l1.x, f0.x, l1.y * f0.y);
+                const float i00 = fmaf(l0.x, f0.y, -l0.y * f0.x), i11 = fmaf(l1.x, f1.y, -l1.y * f1.x);
+                acc[0] += i01 + i10;     // X
+                acc[1] += r10 - r01;     // Y
+                acc[2] += i00 - i11;     // Z
+                acc[3] -= i00 + i11;     // global phase
+                sf[i0] = cmul_add(W.u[0], W.u[1], f0, W.u[2], W.u[3], f1);
+                sf[i1] = cmul_add(W.u[4], W.u[5], f0, W.u[6], W.u[7], f1);
+                sl[i0] = cmul_add(W.u[0], W.u[1], l0, W.u[2], W.u[3], l1);
+                sl[i1] = cmul_add(W.u[4], W.u[5], l0, W.u[6], W.u[7], l1);
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (W.row[m] < 0) continue;
+                float v = acc[m];
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+                if (lane == 0) sacc[(warp * ADJ_GROUP_MAX_BITS + w) * 4 + m] += (double)v;
+            }
+            __syncthreads();
+        }
+        for (int i = tid; i < T; i += ADJ_GROUP_THREADS) {
+            const uint64_t o = base | lo_tab[i & lomask] | hi_tab[i >> nlo];
+            phi[o] = sf[i];
+            lam[o] = sl[i];
+        }
+        __syncthreads();
+    }
+    for (int k = tid; k < p.nwires * 4; k += ADJ_GROUP_THREADS) {
+        const int w = k >> 2, m = k & 3;
+        if (p.w[w].row[m] < 0) continue;
+        double t = 0.0;
+        for (int v = 0; v < ADJ_GROUP_WARPS; ++v) t += sacc[(v * ADJ_GROUP_MAX_BITS + w) * 4 + m];
+        double* row = partial + (size_t)p.w[w].row[m] * p.nb;
+        row[blockIdx.x] = t;
+        for (int c = blockIdx.x + gridDim.x; c < p.nb; c += gridDim.x) row[c] = 0.0;
+    }
+}
+
+static int launch_adj_group_f32(qgpu_handle* h, float2* phi, float2* lam, const AdjGroupParamsF& p,
+                                double* partial) {
+    const size_t smem = adj_group_f32_smem(p.nbits);
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        k_adj_group_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_group_f32_smem(ADJ_GROUP_MAX_BITS));
+    QGPU_CUDA(attr);
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adj_group_f32, ADJ_GROUP_THREADS, smem) != cudaSuccess || occ < 1)
+        occ = 1;
+    const uint64_t grid = std::max<uint64_t>(
+        1, std::min<uint64_t>({p.ngroups, (uint64_t)h->sm_count * occ, (uint64_t)p.nb}));
+    return adj_profiled(h, "k_adj_group_f32", 32.0 * (double)h->dim, [&]() -> int {
+        k_adj_group_f32<<<(unsigned)grid, ADJ_GROUP_THREADS, smem, h->stream>>>(phi, lam, p, partial);
+        QGPU_CHECK_LAUNCH("k_adj_group_f32");
+        h->launches++;
+        h->h2d_bytes += sizeof(p);
+        return QGPU_OK;
+    });
+}
+
+// The passes of a grouped sweep: wires (bits) in ascending order, each pass a tile of up to
+// ADJ_GROUP_MAX_BITS bits that always holds bits 0..4 (32 consecutive amplitudes per load) and
+// is filled up with the lowest other bits. Returns per pass the tile mask and the wires (indices
+// into `bits`) it takes.
+static std::vector<std::pair<uint64_t, std::vector<size_t>>> adj_group_passes(const std::vector<int>& bits, int n) {
+    std::vector<size_t> order(bits.size());
+    for (size_t w = 0; w < order.size(); ++w) order[w] = w;
+    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return bits[x] < bits[y]; });
+    const int kmax = std::min(n, ADJ_GROUP_MAX_BITS);
+    const uint64_t low = (1ull << std::min(n, 5)) - 1;
+    std::vector<std::pair<uint64_t, std::vector<size_t>>> out;
+    size_t i = 0;
+    while (i < order.size()) {
+        uint64_t mask = low;
+        std::vector<size_t> chosen;
+        while (i < order.size() && __builtin_popcountll(mask | (1ull << bits[order[i]])) <= kmax) {
+            mask |= 1ull << bits[order[i]];
+            chosen.push_back(order[i++]);
+        }
+        for (int b = 0; b < n && __builtin_popcountll(mask) < kmax; ++b) mask |= 1ull << b;
+        out.emplace_back(mask, std::move(chosen));
+    }
+    return out;
+}
+
 template <int K>
 static int launch_adj_tile(qgpu_handle* h, double2* phi, double2* lam, const AdjTileParams& p,
                            double* partial) {
@@ -570,8 +733,9 @@ static int launch_adj_tile(qgpu_handle* h, double2* phi, double2* lam, const Adj
 // writes are coalesced, reads follow the map. A CNot ring (the ansatz's entangler, a chain of
 // dependent gates the register-tile passes can only take two at a time) becomes one pass.
 // ---------------------------------------------------------------------------------------------
+template <class T>
 __global__ void __launch_bounds__(ADJ_THREADS)
-k_linperm(const double2* __restrict__ src, double2* __restrict__ dst, uint64_t dim,
+k_linperm(const T* __restrict__ src, T* __restrict__ dst, uint64_t dim,
           const uint64_t* __restrict__ tabs, int nchunks, uint64_t d) {
     extern __shared__ uint64_t tsm[];
     for (int i = threadIdx.x; i < nchunks * 256; i += ADJ_THREADS) tsm[i] = tabs[i];
@@ -606,10 +770,11 @@ static int adj_blocks(const qgpu_handle* h, uint64_t work) {
 }
 
 // Energy of the vector at `psi` into *energy; lambda = H psi left at `lam`.
-static int energy_into(qgpu_handle* h, const double2* psi, double2* lam, const Ham& H,
-                       double* partial, double* energy) {
+template <class T>
+static int energy_into(qgpu_handle* h, const T* psi, T* lam, const Ham& H, double* partial,
+                       double* energy) {
     const int nb = adj_blocks(h, h->dim);
-    k_apply_zzx<<<nb, ADJ_THREADS, 0, h->stream>>>(psi, lam, h->dim, H, partial);
+    k_apply_zzx<T><<<nb, ADJ_THREADS, 0, h->stream>>>(psi, lam, h->dim, H, partial);
     QGPU_CHECK_LAUNCH("k_apply_zzx");
     h->launches++;
     k_sum_partials<<<1, 32, 0, h->stream>>>(partial, nb, 1, partial + nb);
@@ -624,13 +789,154 @@ static int ham_from(const qgpu_handle* h, const double* a, const double* b, Ham*
     if (!a || !b) return fail(QGPU_ERR_INVALID, "observable coefficients are NULL");
     if (h->n_qubits > MAX_HAM_QUBITS)
         return fail(QGPU_ERR_UNSUPPORTED, "observable supports at most 40 qubits");
-    if (h->precision != QGPU_C128)
-        return fail(QGPU_ERR_UNSUPPORTED, "energies and gradients need a complex128 state");
     std::memset(H, 0, sizeof(Ham));
     H->n = h->n_qubits;
     for (int i = 0; i < H->n; ++i) {
         H->a[i] = a[i];
         H->b[i] = b[i];
+    }
+    return QGPU_OK;
+}
+
+// The adjoint sweep of a complex64 handle (the forward pass has run on the register): phi and
+// lambda as complex64 work vectors, every run of single-wire gates in grouped passes
+// (k_adj_group_f32), runs of multi-wire gates undone as one index gather (k_linperm) or through
+// the register-tile passes. The gradients are formed on the host from the Pauli sums, as in the
+// complex128 sweep.
+static int adjoint_sweep_c64(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const Ham& H,
+                             double* energy, double* grads) {
+    size_t nrot = 0;
+    for (size_t g = 0; g < n_ops; ++g) nrot += is_rotation(ops[g].kind) ? 1 : 0;
+    const int nb = adj_blocks(h, h->dim);  // row length of the partial sums (covers every grid)
+    const size_t vec = h->dim * 8;
+    const size_t nrow_cap = 4 * nrot + 4;
+    const size_t part_doubles = (nrow_cap + 1) * (size_t)nb + nrow_cap + 64;
+    int st = h->work2.ensure(2 * vec + part_doubles * 8 + 512);
+    if (st != QGPU_OK) return st;
+    float2* phi = (float2*)h->work2.ptr;
+    float2* lam = (float2*)((uint8_t*)h->work2.ptr + vec);
+    double* partial = (double*)((uint8_t*)h->work2.ptr + 2 * vec);
+    double* gsum = partial + (nrow_cap + 1) * (size_t)nb;
+    QGPU_CUDA(cudaMemcpyAsync(phi, h->state, vec, cudaMemcpyDeviceToDevice, h->stream));
+    st = energy_into(h, (const float2*)phi, lam, H, partial + nrow_cap * (size_t)nb, energy);
+    if (st != QGPU_OK) return st;
+    std::vector<std::vector<std::pair<int, double>>> terms(n_ops);
+    int nrows = 0;
+    std::vector<qgpu_op> seg;  // consecutive multi-wire gates, undone together
+    float2* spare = nullptr;   // third vector for out-of-place index permutations
+    auto flush_seg = [&]() -> int {
+        if (seg.empty()) return QGPU_OK;
+        std::vector<uint64_t> tabs;
+        uint64_t d = 0;
+        if (h->n_qubits >= 10 && seg.size() >= 3 &&
+            affine_tables(seg.data(), seg.size(), h->n_qubits, &tabs, &d)) {
+            if (!spare && h->work3.ensure(vec) == QGPU_OK) spare = (float2*)h->work3.ptr;
+            if (spare && h->tables.ensure(tabs.size() * 8) == QGPU_OK) {
+                QGPU_CUDA(copy_async(h, h->tables.ptr, tabs.data(), tabs.size() * 8,
+                                     cudaMemcpyHostToDevice));
+                const int nch = (h->n_qubits + 7) / 8;
+                const int blocks = adj_blocks(h, h->dim);
+                for (float2** v : {&phi, &lam}) {
+                    k_linperm<float2><<<blocks, ADJ_THREADS, nch * 256 * 8, h->stream>>>(
+                        *v, spare, h->dim, (const uint64_t*)h->tables.ptr, nch, d);
+                    QGPU_CHECK_LAUNCH("k_linperm");
+                    h->launches++;
+                    std::swap(*v, spare);
+                }
+                seg.clear();
+                return QGPU_OK;
+            }
+        }
+        Plan plan;
+        int s2 = build_plan(seg.data(), seg.size(), h->n_qubits, nullptr, 0, nullptr, 0,
+                            plan_options_for(h), &plan);
+        if (s2 == QGPU_OK) s2 = run_plan_on(h, phi, plan, false, false);
+        if (s2 == QGPU_OK) s2 = run_plan_on(h, lam, plan, false, false);
+        seg.clear();
+        return s2;
+    };
+    std::vector<size_t> run;  // op indices of the current single-wire run, in reverse order
+    auto flush_run = [&]() -> int {
+        if (run.empty()) return QGPU_OK;
+        std::vector<int> wires;                  // bit of each wire, in first-seen order
+        std::vector<std::vector<size_t>> gates;  // per wire, its ops in reverse order
+        for (size_t gi : run) {
+            const int bit = h->n_qubits - 1 - ops[gi].target;
+            size_t w = std::find(wires.begin(), wires.end(), bit) - wires.begin();
+            if (w == wires.size()) {
+                wires.push_back(bit);
+                gates.emplace_back();
+            }
+            gates[w].push_back(gi);
+        }
+        run.clear();
+        std::vector<PauliRun> prs(wires.size());
+        for (size_t w = 0; w < wires.size(); ++w) {
+            int s3 = pauli_run(ops, gates[w], h->n_qubits, &prs[w]);
+            if (s3 != QGPU_OK) return s3;
+        }
+        for (const auto& pass : adj_group_passes(wires, h->n_qubits)) {
+            AdjGroupParamsF p;
+            std::memset(&p, 0, sizeof(p));
+            for (int b = 0; b < 64; ++b)
+                if ((pass.first >> b) & 1ull) p.bits[p.nbits++] = b;
+            p.ngroups = h->dim >> p.nbits;
+            p.nb = nb;
+            p.nwires = (int)pass.second.size();
+            for (int c = 0; c < p.nwires; ++c) {
+                const size_t w = pass.second[c];
+                AdjGroupWireF& gw = p.w[c];
+                gw.lb = (int)(std::find(p.bits, p.bits + p.nbits, wires[w]) - p.bits);
+                int kind_row[5] = {-1, -1, -1, -1, -1};
+                for (int m = 1; m <= 4; ++m) {
+                    gw.row[m - 1] = -1;
+                    if (prs[w].need[m]) gw.row[m - 1] = kind_row[m] = nrows++;
+                }
+                for (int e = 0; e < 4; ++e) {
+                    gw.u[2 * e] = (float)prs[w].undo[e].real();
+                    gw.u[2 * e + 1] = (float)prs[w].undo[e].imag();
+                }
+                for (const auto& r : prs[w].rots)
+                    for (int m = 1; m <= 4; ++m)
+                        if (r.second[m] != 0.0) terms[r.first].emplace_back(kind_row[m], r.second[m]);
+            }
+            int s2 = launch_adj_group_f32(h, phi, lam, p, partial);
+            if (s2 != QGPU_OK) return s2;
+        }
+        return QGPU_OK;
+    };
+    for (size_t gi = n_ops; gi-- > 0;) {
+        const qgpu_op& op = ops[gi];
+        if (op.kind == QGPU_GATE_ID) continue;
+        int k = 1;
+        op_arity(op, h->n_qubits, &k);
+        if (k > 1) {
+            st = flush_run();
+            if (st != QGPU_OK) return st;
+            seg.push_back(inverse_op(op));
+            continue;
+        }
+        st = flush_seg();
+        if (st != QGPU_OK) return st;
+        run.push_back(gi);
+    }
+    st = flush_run();
+    if (st != QGPU_OK) return st;
+    st = flush_seg();
+    if (st != QGPU_OK) return st;
+    if (nrows > (int)nrow_cap) return fail(QGPU_ERR_UNSUPPORTED, "adjoint: partial-sum rows overflow");
+    if (nrows) {
+        k_sum_partials<<<(unsigned)((nrows + 3) / 4), 128, 0, h->stream>>>(partial, nb, nrows, gsum);
+        QGPU_CHECK_LAUNCH("k_sum_partials");
+        h->launches++;
+    }
+    std::vector<double> gr(nrows);
+    if (nrows) QGPU_CUDA(copy_async(h, gr.data(), gsum, (size_t)nrows * 8, cudaMemcpyDeviceToHost));
+    QGPU_CUDA(cudaStreamSynchronize(h->stream));
+    for (size_t g = 0; g < n_ops; ++g) {
+        double v = 0.0;
+        for (const auto& t : terms[g]) v += t.second * gr[t.first];
+        grads[g] = v;
     }
     return QGPU_OK;
 }
@@ -647,11 +953,13 @@ int qgpu_expectation_zzx(qgpu_handle* h, const double* a, const double* b, doubl
     int st = ham_from(h, a, b, &H);
     if (st != QGPU_OK) return st;
     const int nb = adj_blocks(h, h->dim);
-    st = h->work2.ensure(h->dim * 16 + (size_t)(nb + 8) * 8 + 256);
+    const size_t vec = h->dim * h->amp_bytes;
+    st = h->work2.ensure(vec + (size_t)(nb + 8) * 8 + 256);
     if (st != QGPU_OK) return st;
-    double2* lam = (double2*)h->work2.ptr;
-    double* partial = (double*)((uint8_t*)h->work2.ptr + h->dim * 16);
-    return energy_into(h, (const double2*)h->state, lam, H, partial, energy);
+    double* partial = (double*)((uint8_t*)h->work2.ptr + vec);
+    if (h->precision == QGPU_C64)
+        return energy_into(h, (const float2*)h->state, (float2*)h->work2.ptr, H, partial, energy);
+    return energy_into(h, (const double2*)h->state, (double2*)h->work2.ptr, H, partial, energy);
 }
 
 int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const double* mats,
@@ -673,6 +981,7 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
     // forward pass on the register
     st = qgpu_apply_program(h, ops, n_ops, mats, n_mat_doubles, none_flags, n_none_flags);
     if (st != QGPU_OK) return st;
+    if (h->precision == QGPU_C64) return adjoint_sweep_c64(h, ops, n_ops, H, energy, grads);
     // work vectors: phi (copy of psi_L), lambda, block partials per rotation
     size_t nrot = 0;
     for (size_t g = 0; g < n_ops; ++g) nrot += is_rotation(ops[g].kind) ? 1 : 0;
@@ -729,7 +1038,7 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
                 const int nch = (h->n_qubits + 7) / 8;
                 const int blocks = adj_blocks(h, h->dim);
                 for (double2** v : {&phi, &lam}) {
-                    k_linperm<<<blocks, ADJ_THREADS, nch * 256 * 8, h->stream>>>(
+                    k_linperm<double2><<<blocks, ADJ_THREADS, nch * 256 * 8, h->stream>>>(
                         *v, spare, h->dim, (const uint64_t*)h->tables.ptr, nch, d);
                     QGPU_CHECK_LAUNCH("k_linperm");
                     h->launches++;
@@ -795,20 +1104,9 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
                 int s3 = pauli_run(ops, gates[w], h->n_qubits, &prs[w]);
                 if (s3 != QGPU_OK) return s3;
             }
-            std::vector<size_t> order(wires.size());
-            for (size_t w = 0; w < order.size(); ++w) order[w] = w;
-            std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return wires[x] < wires[y]; });
-            const int kmax = std::min(h->n_qubits, ADJ_GROUP_MAX_BITS);
-            const uint64_t low = (1ull << std::min(h->n_qubits, 5)) - 1;  // coalescing: bits 0..4 in every tile
-            size_t i = 0;
-            while (i < order.size()) {
-                uint64_t mask = low;
-                std::vector<size_t> chosen;
-                while (i < order.size() && __builtin_popcountll(mask | (1ull << wires[order[i]])) <= kmax) {
-                    mask |= 1ull << wires[order[i]];
-                    chosen.push_back(order[i++]);
-                }
-                for (int b = 0; b < h->n_qubits && __builtin_popcountll(mask) < kmax; ++b) mask |= 1ull << b;
+            for (const auto& pass : adj_group_passes(wires, h->n_qubits)) {
+                const uint64_t mask = pass.first;
+                const std::vector<size_t>& chosen = pass.second;
                 AdjGroupParams p;
                 std::memset(&p, 0, sizeof(p));
                 for (int b = 0; b < 64; ++b)

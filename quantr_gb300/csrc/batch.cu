@@ -5,8 +5,9 @@
 // takes circuit after circuit from an atomic work counter (no CTA ever waits on another) and runs
 // the forward pass, lambda = H psi, the energy and the adjoint reverse sweep entirely in shared
 // memory. Larger circuits run one after another through the register-tile passes and
-// qgpu_adjoint_grad on a handle per register size, with the float-pair fusion budget picked per
-// size bucket by timing the candidates on the bucket's first circuit.
+// qgpu_adjoint_grad on a handle per register size in the batch's precision, with the fusion
+// budget (and, for complex128, the adjoint sweep form) picked per size bucket by timing the
+// candidates on the bucket's first circuit.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -355,14 +356,17 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
             const qgpu_batch_item& it = items[i];
             if (budget.count(it.n_qubits)) continue;
             qgpu_handle* h = nullptr;
-            st = qgpu_create(it.n_qubits, QGPU_C128, &h);
+            st = qgpu_create(it.n_qubits, precision, &h);
             if (st != QGPU_OK) break;
             tune[it.n_qubits] = h;
             const qgpu_op* po = ops + it.op_offset;
-            static const int cand[] = {100, 140, 200, 280};
+            // candidates of the float-pair (complex128) or f32 (complex64) fusion budget
+            static const int cand128[] = {100, 140, 200, 280}, cand64[] = {24, 48, 96, 160};
+            const int* cand = precision == QGPU_C128 ? cand128 : cand64;
             double best = 1e30;
-            int pick = 280;
-            for (int b : cand) {
+            int pick = cand[3];
+            for (int ci = 0; ci < 4; ++ci) {
+                const int b = cand[ci];
                 h->batch_budget = b;
                 qgpu_set_zero(h);
                 auto t0 = std::chrono::steady_clock::now();
@@ -377,10 +381,12 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
             if (st != QGPU_OK) break;
             budget[it.n_qubits] = pick;
             h->batch_budget = pick;
-            // the sweep form: a first (untimed) gradient allocates the work vectors
+            // the sweep form (complex128; complex64 sweeps are always grouped): a first (untimed)
+            // gradient allocates the work vectors
             std::vector<double> g((size_t)std::max(1, it.n_ops));
             double e = 0.0, tsweep[2] = {0.0, 0.0};
-            for (int form : {1, 1, 0}) {
+            const std::vector<int> forms = precision == QGPU_C128 ? std::vector<int>{1, 1, 0} : std::vector<int>{};
+            for (int form : forms) {
                 h->adj_group = form;
                 qgpu_set_zero(h);
                 auto t0 = std::chrono::steady_clock::now();
@@ -390,7 +396,7 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
                 tsweep[form] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             }
             if (st != QGPU_OK) break;
-            sweep[it.n_qubits] = tsweep[1] <= tsweep[0] ? 1 : 0;
+            sweep[it.n_qubits] = precision == QGPU_C128 ? (tsweep[1] <= tsweep[0] ? 1 : 0) : 1;
             if (tuned_budget) tuned_budget[it.n_qubits] = pick + (sweep[it.n_qubits] ? 65536 : 0);
         }
         for (auto& kv : tune) qgpu_destroy(kv.second);
@@ -412,7 +418,7 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
             const qgpu_batch_item& it = items[i];
             qgpu_handle*& h = handles[it.n_qubits];
             int st = QGPU_OK;
-            if (!h) st = qgpu_create(it.n_qubits, QGPU_C128, &h);
+            if (!h) st = qgpu_create(it.n_qubits, precision, &h);
             if (st == QGPU_OK) {
                 h->batch_budget = budget[it.n_qubits];
                 h->adj_group = sweep[it.n_qubits];

@@ -1920,7 +1920,7 @@ PlanOptions plan_options_for(const qgpu_handle* h) {
     // layout the 30-qubit brickwork+QFT step measured 2549 ms at 280 against 3625 ms at 140
     // (one dense step per pass) on GB300.
     if (o.policy == POL_FF) o.budget = h->batch_budget > 0 ? h->batch_budget : env_int("QGPU_FF_BUDGET", 280);
-    else if (o.policy == POL_F32) o.budget = env_int("QGPU_F32_BUDGET", 48);
+    else if (o.policy == POL_F32) o.budget = h->batch_budget > 0 ? h->batch_budget : env_int("QGPU_F32_BUDGET", 48);
     else o.budget = env_int("QGPU_F64_BUDGET", 1 << 20);
     o.max_bits = std::max(2, std::min(env_int("QGPU_TILE_BITS", MAX_TILE_BITS), MAX_TILE_BITS));
     // float-pair arithmetic on 8 amplitudes per thread needs ~120 registers (2 CTAs per SM):

@@ -195,6 +195,26 @@ def test_grouped_sweep_equals_per_wire_passes(monkeypatch, n, layers):
     assert np.max(np.abs(g1 - g2)) <= 1e-11
 
 
+@pytest.mark.parametrize("n,layers", [(9, 3), (14, 4), (21, 2)])
+def test_complex64_energy_and_gradient(n, layers):
+    """complex64 handles: the forward pass in f32, the sweep in k_adj_group_f32 (grouped passes
+    at every size) and k_linperm for the CNot rings; energies within 1e-5 and gradients within
+    1e-4 of the complex128 adjoint."""
+    an = W.ansatz(n=n, layers=layers, seed=3)
+    prog = an.program()
+    h128 = nat.Handle(n)
+    e128, g128 = GR.energy_and_gradient(h128, prog, an.a, an.b)
+    h128.close()
+    h64 = nat.Handle(n, nat.QGPU_C64)
+    h64.set_profiling(True)
+    e64, g64 = GR.energy_and_gradient(h64, prog, an.a, an.b)
+    prof = h64.profile(reset=True)
+    h64.close()
+    assert prof["k_adj_group_f32"][0] >= layers, prof
+    assert abs(e64 - e128) <= 1e-5
+    assert np.max(np.abs(g64 - g128)) <= 1e-4
+
+
 def test_adjoint_rejects_custom():
     b = ProgramBuilder(3)
     b.add("H", 0)

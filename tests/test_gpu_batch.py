@@ -2,7 +2,8 @@
 
 Bars: batched complex128 energies and gradients equal the per-circuit qgpu_adjoint_grad results
 within 1e-10 (the in-shared-memory path uses f64 with a different reduction order); complex64
-energies and gradients within 1e-4.
+energies and gradients (shared-memory path up to 13 qubits, complex64 register passes and the f32
+grouped sweep above) within 1e-4 of complex128.
 """
 import numpy as np
 import pytest
@@ -41,12 +42,13 @@ def test_batch_c128_matches_per_circuit():
     for a, b in zip(g, rg):
         assert np.max(np.abs(a - b)) <= 1e-10
     assert tuned and all(q > 12 for q in tuned)
-    assert all(t["adjoint_sweep"] in ("grouped", "per-wire") and t["ff_budget"] > 0 for t in tuned.values())
+    assert all(t["adjoint_sweep"] in ("grouped", "per-wire") and t["fusion_budget"] > 0 for t in tuned.values())
 
 
 def test_batch_c64_energies_and_gradients():
-    """complex64 batches (in shared memory up to 13 qubits, register passes above) against the
-    complex128 per-circuit adjoint: energies and every gradient entry within 1e-4."""
+    """complex64 batches (in shared memory up to 13 qubits, complex64 register passes and the f32
+    grouped sweep above) against the complex128 per-circuit adjoint: energies and every gradient
+    entry within 1e-4."""
     cs = B.batch_config(count=24, seed=6, layers=2, n_min=4, n_max=16)
     assert {c.n for c in cs} & {14, 15, 16}
     e64, g64, _ = B.run_batch(cs, precision=nat.QGPU_C64)
