@@ -734,6 +734,53 @@ __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, co
         } else if constexpr (ONE == ST_REAL && IsArith<P>::value) {
 #pragma unroll
             for (int u = 0; u < U; ++u) P::real(v[u][0], v[u][1], p.steps[0]);
+        } else if constexpr (ONE == ST_TABLE && IsArith<P>::value) {
+            // QFT rows: unconditional REAL / DENSE steps and phase tables only (no dispatch over
+            // the other step kinds, no control test on the 2x2 steps)
+            for (int s = 0; s < p.nsteps; ++s) {
+                const DevStep& sp = p.steps[s];
+                if (sp.type == ST_TABLE) {
+#pragma unroll
+                    for (int u = 0; u < U; ++u)
+#pragma unroll
+                        for (int j = 0; j < T; ++j) {
+                            const uint64_t idx = base[u] | off[j];
+                            if ((idx & sp.cm) != sp.cm) continue;
+#pragma unroll
+                            for (int f = 0; f < MAX_TABLE_FIELDS; ++f) {
+                                if (f >= sp.nfields) break;
+                                const uint32_t y = (uint32_t)((idx >> sp.tab_shift[f]) &
+                                                              ((1ull << sp.tab_width[f]) - 1ull));
+                                P::mul_table(v[u][j], p, sp.tab_off[f] + y);
+                            }
+                        }
+                } else {
+                    const bool dense = sp.type == ST_DENSE;
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        if constexpr (K == 1) {
+                            if (dense) P::dense(v[u][0], v[u][1], sp);
+                            else P::real(v[u][0], v[u][1], sp);
+                        } else if (sp.lb == 0) {
+                            if (dense) {
+                                P::dense(v[u][0], v[u][1], sp);
+                                P::dense(v[u][2], v[u][3], sp);
+                            } else {
+                                P::real(v[u][0], v[u][1], sp);
+                                P::real(v[u][2], v[u][3], sp);
+                            }
+                        } else {
+                            if (dense) {
+                                P::dense(v[u][0], v[u][2], sp);
+                                P::dense(v[u][1], v[u][3], sp);
+                            } else {
+                                P::real(v[u][0], v[u][2], sp);
+                                P::real(v[u][1], v[u][3], sp);
+                            }
+                        }
+                    }
+                }
+            }
         } else {
             for (int s = 0; s < p.nsteps; ++s) {
                 const DevStep& sp = p.steps[s];
@@ -1084,6 +1131,21 @@ static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
             all_dense = p.steps[i].type == ST_DENSE && p.steps[i].cm == 0;
         if (all_dense) {
             k_tile<K, U, P, ST_DENSE><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
+            launched = true;
+        }
+    }
+    if constexpr ((K == 1 || K == 2) && IsArith<P>::value) {
+        // passes of unconditional 2x2 steps and phase tables only (the QFT rows): straight-line
+        // variant; tuning knob QGPU_TABLE_STRAIGHT=0 keeps the step loop
+        static const int straight_tab = env_int("QGPU_TABLE_STRAIGHT", 1);
+        bool ok = !launched && straight_tab != 0, any_table = false;
+        for (int i = 0; i < p.nsteps && ok; ++i) {
+            const DevStep& d = p.steps[i];
+            any_table = any_table || d.type == ST_TABLE;
+            ok = d.type == ST_TABLE || ((d.type == ST_DENSE || d.type == ST_REAL) && d.cm == 0);
+        }
+        if (ok && any_table) {
+            k_tile<K, U, P, ST_TABLE><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
             launched = true;
         }
     }
