@@ -215,6 +215,40 @@ def test_complex64_energy_and_gradient(n, layers):
     assert np.max(np.abs(g64 - g128)) <= 1e-4
 
 
+def test_complex64_all_gate_kinds_and_permutation_runs():
+    """complex64 sweep on every invertible gate kind (fixed gates inside single-wire runs, the
+    multi-wire kinds through the register passes) and on CNot rings / X / Swap runs (the index
+    gather out of place, into and out of the third vector): energy and every gradient against
+    the complex128 adjoint, 1e-5 / 1e-4; the register holds the final state afterwards."""
+    n = 12
+    rng = np.random.default_rng(31)
+    b = ProgramBuilder(n)
+    for layer in range(3):
+        for w in range(n):
+            b.add(["Rx", "Ry", "Rz", "Phase"][(w + layer) % 4], w, (), param=rng.uniform(-3, 3))
+        b.add("H", 0); b.add("S", 1); b.add("T", 2); b.add("Sdag", 3); b.add("Tdag", 4)
+        b.add("X90", 5); b.add("Y90", 6); b.add("MX90", 7); b.add("MY90", 8); b.add("Y", 9)
+        b.add("CNot", 1, (0,)); b.add("CZ", 2, (4,)); b.add("CY", 5, (3,)); b.add("Swap", 0, (5,))
+        b.add("CR", 3, (1,), param=0.37); b.add("CRk", 4, (2,), k=3); b.add("Toffoli", 1, (3, 5))
+        for w in range(n):
+            b.add("Ry", w, (), param=rng.uniform(-3, 3))
+        for w in range(n):
+            b.add("CNot", (w + 1) % n, (w,))
+        b.add("X", 3); b.add("Swap", 2, (9,)); b.add("CNot", 0, (7,))
+    prog = b.build()
+    a_c = rng.normal(size=n)
+    b_c = rng.normal(size=n)
+    h128 = nat.Handle(n)
+    e128, g128 = GR.energy_and_gradient(h128, prog, a_c, b_c)
+    h64 = nat.Handle(n, nat.QGPU_C64)
+    e64, g64 = GR.energy_and_gradient(h64, prog, a_c, b_c)
+    assert abs(e64 - e128) <= 1e-5
+    assert np.max(np.abs(g64 - g128)) <= 1e-4
+    assert np.max(np.abs(h64.download() - h128.download())) <= 1e-5
+    h64.close()
+    h128.close()
+
+
 def test_adjoint_rejects_custom():
     b = ProgramBuilder(3)
     b.add("H", 0)
