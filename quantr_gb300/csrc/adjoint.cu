@@ -539,9 +539,7 @@ static int adj_profiled(qgpu_handle* h, const char* name, double bytes, F&& laun
 static int launch_adj_group(qgpu_handle* h, double2* phi, double2* lam, const AdjGroupParams& p,
                             double* partial) {
     const size_t smem = adj_group_smem(p.nbits);
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        k_adj_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_group_smem(ADJ_GROUP_MAX_BITS));
-    QGPU_CUDA(attr);
+    QGPU_CUDA(smem_opt_in((const void*)k_adj_group, adj_group_smem(ADJ_GROUP_MAX_BITS)));
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adj_group, ADJ_GROUP_THREADS, smem) != cudaSuccess || occ < 1)
         occ = 1;
@@ -671,9 +669,7 @@ k_adj_group_f32(float2* __restrict__ phi, float2* __restrict__ lam,
 static int launch_adj_group_f32(qgpu_handle* h, float2* phi, float2* lam, const AdjGroupParamsF& p,
                                 double* partial) {
     const size_t smem = adj_group_f32_smem(p.nbits);
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        k_adj_group_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_group_f32_smem(ADJ_GROUP_MAX_BITS));
-    QGPU_CUDA(attr);
+    QGPU_CUDA(smem_opt_in((const void*)k_adj_group_f32, adj_group_f32_smem(ADJ_GROUP_MAX_BITS)));
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adj_group_f32, ADJ_GROUP_THREADS, smem) != cudaSuccess || occ < 1)
         occ = 1;

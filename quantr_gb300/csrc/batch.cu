@@ -307,9 +307,9 @@ extern "C" int qgpu_batch_run(const qgpu_batch_item* items, size_t n_items, cons
         BATCH_TRY(cudaMemcpyAsync(d_obs, obs, n_obs * sizeof(double), cudaMemcpyHostToDevice, s));
         BATCH_TRY(cudaStreamSynchronize(s));
         if (precision == QGPU_C128)
-            BATCH_TRY(cudaFuncSetAttribute(k_batch_small<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            BATCH_TRY(smem_opt_in((const void*)k_batch_small<double2>, smem));
         else
-            BATCH_TRY(cudaFuncSetAttribute(k_batch_small<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            BATCH_TRY(smem_opt_in((const void*)k_batch_small<float2>, smem));
         // capture: counter reset + persistent kernel, replayed as one graph
         BATCH_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         cudaMemsetAsync(d_cnt, 0, sizeof(unsigned), s);

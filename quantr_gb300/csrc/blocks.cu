@@ -215,8 +215,7 @@ static int launch_block_ff_t(qgpu_handle* h, const BlockArgs& a) {
     const size_t smem = (size_t)(D * D + D * BFF_GT) * 16;
     // set once per kernel instance; a function-local static initialises once even when
     // several host threads launch concurrently
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_block_ff<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const cudaError_t attr = smem_opt_in((const void*)k_block_ff<D>, smem);
     QGPU_CUDA(attr);
     const uint64_t ntiles = (a.ngroups + BFF_GT - 1) / BFF_GT;
     uint64_t blocks = std::min<uint64_t>(ntiles, (uint64_t)h->sm_count * 2);
@@ -245,8 +244,7 @@ static int launch_block_t(qgpu_handle* h, const BlockArgs& a) {
     const size_t smem = (size_t)(D * D + D * BLK_GT) * sizeof(T);
     // set once per kernel instance; a function-local static initialises once even when
     // several host threads launch concurrently
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_block<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const cudaError_t attr = smem_opt_in((const void*)k_block<T, D>, smem);
     QGPU_CUDA(attr);
     const uint64_t ntiles = (a.ngroups + BLK_GT - 1) / BLK_GT;
     uint64_t blocks = std::min<uint64_t>(ntiles, (uint64_t)h->sm_count * 2);

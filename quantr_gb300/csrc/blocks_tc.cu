@@ -269,8 +269,7 @@ int launch_tc(qgpu_handle* h, const DenseBlock& b, const uint8_t* dev_img) {
     using SH = TcbShape<D>;
     // set once per kernel instance; a function-local static initialises once even when
     // several host threads launch concurrently
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_block_tc<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SH::SMEM);
+    const cudaError_t attr = smem_opt_in((const void*)k_block_tc<D>, SH::SMEM);
     QGPU_CUDA(attr);
     TcBlockArgs a;
     std::memset(&a, 0, sizeof(a));

@@ -552,8 +552,7 @@ bool dg_supported(const qgpu_handle* h) {
 
 int dg_launch_pass(qgpu_handle* h, const int bits[4], const uint32_t* bimg,
                    const int32_t (*kap)[dg::KAP]) {
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_dg2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM);
+    const cudaError_t attr = smem_opt_in((const void*)k_dg2, DG_SMEM);
     QGPU_CUDA(attr);
     DgArgs a;
     a.nblocks = (h->dim >> 4) / DG_M;

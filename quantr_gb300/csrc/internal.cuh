@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <map>
+#include <mutex>
 #include <utility>
 #include <string>
 #include <vector>
@@ -31,6 +32,23 @@ int cuda_fail(cudaError_t e, const char* what);
         cudaError_t e_ = cudaGetLastError();                        \
         if (e_ != cudaSuccess) return ::qgpu::cuda_fail(e_, what);  \
     } while (0)
+
+// Opts `kernel` into `bytes` of dynamic shared memory on the current device. The attribute
+// belongs to the device's context, so it is set once per (kernel, device) and again when a
+// larger size is asked for; safe from several host threads.
+inline cudaError_t smem_opt_in(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& have = done[{kernel, dev}];
+    if (have >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) have = bytes;
+    return e;
+}
 
 // Device scratch owned by a handle, grown on demand and reused across calls.
 struct Scratch {

@@ -568,11 +568,9 @@ static void build_pair_tc_image(const Plan& plan, const Pass& ps, const uint64_t
 
 int launch_pair2_tc(qgpu_handle* h, const Plan& plan, const Pass& ps, const uint64_t pre_off[16],
                     const uint64_t post_off[16], int variant) {
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_pair2_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PTC_SMEM);
+    const cudaError_t attr = smem_opt_in((const void*)k_pair2_tc, PTC_SMEM);
     QGPU_CUDA(attr);
-    static const cudaError_t attr_ws =
-        cudaFuncSetAttribute(k_pair2_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PWS_SMEM);
+    const cudaError_t attr_ws = smem_opt_in((const void*)k_pair2_ws, PWS_SMEM);
     QGPU_CUDA(attr_ws);
     PairTcArgs a;
     std::memset(&a, 0, sizeof(a));

@@ -159,11 +159,8 @@ static int launch_group(qgpu_handle* h, const GroupArgs& a0, const uint8_t* dev_
     const uint64_t cap = (uint64_t)h->sm_count * 8;
     if (blocks > cap) blocks = cap;
     if (smem > 48 * 1024) {
-        cudaError_t e = (h->precision == QGPU_C128)
-                            ? cudaFuncSetAttribute(k_group<double2>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                            : cudaFuncSetAttribute(k_group<float2>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = (h->precision == QGPU_C128) ? smem_opt_in((const void*)k_group<double2>, smem)
+                                                    : smem_opt_in((const void*)k_group<float2>, smem);
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_group)");
     }
     if (h->precision == QGPU_C128)
@@ -901,11 +898,7 @@ template <class P>
 static int launch_tile1_pipe(qgpu_handle* h, const TileParams& p) {
     using S = typename P::S;
     const size_t smem = (size_t)PIPE_STAGES * 2 * PIPE_CH * sizeof(S);
-    // set once per kernel instance; a function-local static initialises once even when
-    // several host threads launch concurrently
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_tile1_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    QGPU_CUDA(attr);
+    QGPU_CUDA(smem_opt_in((const void*)k_tile1_pipe<P>, smem));
     const uint64_t nchunks = h->dim / (2ull * PIPE_CH);
     uint64_t blocks = std::min<uint64_t>(nchunks, (uint64_t)h->sm_count * 3);
     if (blocks < 1) blocks = 1;
