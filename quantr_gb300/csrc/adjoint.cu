@@ -359,7 +359,7 @@ k_adj_tile(double2* __restrict__ phi, double2* __restrict__ lam,
 // taken before its own undo, so the results are those of one pass per wire (k_adj_tile with
 // Pauli steps), with one read and one write of each vector per pass.
 // ---------------------------------------------------------------------------------------------
-constexpr int ADJ_GROUP_MAX_BITS = 11;
+constexpr int ADJ_GROUP_MAX_BITS = ADJ_GROUP_TILE_BITS;
 constexpr int ADJ_GROUP_THREADS = 256;
 constexpr int ADJ_GROUP_WARPS = ADJ_GROUP_THREADS / 32;
 
@@ -684,31 +684,6 @@ static int launch_adj_group_f32(qgpu_handle* h, float2* phi, float2* lam, const 
     });
 }
 
-// The passes of a grouped sweep: wires (bits) in ascending order, each pass a tile of up to
-// ADJ_GROUP_MAX_BITS bits that always holds bits 0..4 (32 consecutive amplitudes per load) and
-// is filled up with the lowest other bits. Returns per pass the tile mask and the wires (indices
-// into `bits`) it takes.
-static std::vector<std::pair<uint64_t, std::vector<size_t>>> adj_group_passes(const std::vector<int>& bits, int n) {
-    std::vector<size_t> order(bits.size());
-    for (size_t w = 0; w < order.size(); ++w) order[w] = w;
-    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return bits[x] < bits[y]; });
-    const int kmax = std::min(n, ADJ_GROUP_MAX_BITS);
-    const uint64_t low = (1ull << std::min(n, 5)) - 1;
-    std::vector<std::pair<uint64_t, std::vector<size_t>>> out;
-    size_t i = 0;
-    while (i < order.size()) {
-        uint64_t mask = low;
-        std::vector<size_t> chosen;
-        while (i < order.size() && __builtin_popcountll(mask | (1ull << bits[order[i]])) <= kmax) {
-            mask |= 1ull << bits[order[i]];
-            chosen.push_back(order[i++]);
-        }
-        for (int b = 0; b < n && __builtin_popcountll(mask) < kmax; ++b) mask |= 1ull << b;
-        out.emplace_back(mask, std::move(chosen));
-    }
-    return out;
-}
-
 template <int K>
 static int launch_adj_tile(qgpu_handle* h, double2* phi, double2* lam, const AdjTileParams& p,
                            double* partial) {
@@ -871,7 +846,7 @@ static int adjoint_sweep_c64(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, c
             int s3 = pauli_run(ops, gates[w], h->n_qubits, &prs[w]);
             if (s3 != QGPU_OK) return s3;
         }
-        for (const auto& pass : adj_group_passes(wires, h->n_qubits)) {
+        for (const auto& pass : adj_group_passes(wires, h->n_qubits, ADJ_GROUP_MAX_BITS)) {
             AdjGroupParamsF p;
             std::memset(&p, 0, sizeof(p));
             for (int b = 0; b < 64; ++b)
@@ -1100,7 +1075,7 @@ int qgpu_adjoint_grad(qgpu_handle* h, const qgpu_op* ops, size_t n_ops, const do
                 int s3 = pauli_run(ops, gates[w], h->n_qubits, &prs[w]);
                 if (s3 != QGPU_OK) return s3;
             }
-            for (const auto& pass : adj_group_passes(wires, h->n_qubits)) {
+            for (const auto& pass : adj_group_passes(wires, h->n_qubits, ADJ_GROUP_MAX_BITS)) {
                 const uint64_t mask = pass.first;
                 const std::vector<size_t>& chosen = pass.second;
                 AdjGroupParams p;

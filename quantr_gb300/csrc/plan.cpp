@@ -1382,6 +1382,29 @@ qgpu_op inverse_op(const qgpu_op& op) {
     return r;
 }
 
+std::vector<std::pair<uint64_t, std::vector<size_t>>> adj_group_passes(const std::vector<int>& bits,
+                                                                       int n, int max_bits) {
+    std::vector<size_t> order(bits.size());
+    for (size_t w = 0; w < order.size(); ++w) order[w] = w;
+    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return bits[x] < bits[y]; });
+    const int kmax = std::min(n, max_bits);
+    const uint64_t low = (1ull << std::min(n, 5)) - 1;
+    std::vector<std::pair<uint64_t, std::vector<size_t>>> out;
+    size_t i = 0;
+    while (i < order.size()) {
+        uint64_t mask = low;
+        std::vector<size_t> chosen;
+        while (i < order.size() && (chosen.empty() ||
+                                    __builtin_popcountll(mask | (1ull << bits[order[i]])) <= kmax)) {
+            mask |= 1ull << bits[order[i]];  // (the first wire always: a pass takes at least one)
+            chosen.push_back(order[i++]);
+        }
+        for (int b = 0; b < n && __builtin_popcountll(mask) < kmax; ++b) mask |= 1ull << b;
+        out.emplace_back(mask, std::move(chosen));
+    }
+    return out;
+}
+
 int pauli_run(const qgpu_op* ops, const std::vector<size_t>& gw, int n, PauliRun* out) {
     const size_t k = gw.size();
     std::vector<std::array<cd, 4>> fwd(k), inv(k);  // row-major 2x2: m[2 l + j]

@@ -52,6 +52,15 @@ struct PauliRun {
 };
 // gw: the run's op indices into ops, in reverse order (gw[0] the run's last gate).
 int pauli_run(const qgpu_op* ops, const std::vector<size_t>& gw, int n, PauliRun* out);
+
+// The passes of a grouped adjoint sweep (the runs of single-wire gates of many wires per pass):
+// wire bits in ascending order, each pass a tile of at most `max_bits` index bits that always
+// holds bits 0..4 (32 consecutive amplitudes per load) and is filled up with the lowest other
+// bits. Returns per pass the tile mask and the wires (indices into `bits`) it takes; every wire
+// lands in exactly one pass.
+constexpr int ADJ_GROUP_TILE_BITS = 11;
+std::vector<std::pair<uint64_t, std::vector<size_t>>> adj_group_passes(const std::vector<int>& bits,
+                                                                       int n, int max_bits);
 // Whether ops (CNot, X, Swap only), applied in order, form an affine index map y -> A y + b over
 // GF(2); if so, the gather tables of its inverse h for one out-of-place pass dst[y] = src[h(y)]:
 // h(y) = *d xor tabs[c * 256 + byte c of y] over the 8-bit chunks c of y.

@@ -7,7 +7,8 @@
 //     Im <lambda| s |phi> (s = X, Y, Z, -I) with the run's coefficients equals the central
 //     difference of the energy <psi|H|psi> (random Hermitian H, random start state);
 //   * affine_tables: a run of CNot / X / Swap as one gather through 8-bit chunk tables equals
-//     the gates applied one by one.
+//     the gates applied one by one;
+//   * adj_group_passes: the grouped sweep's partition of a run's wires into tiles.
 // Prints "fails <n>"; exit code 0 when there are none.
 #include <algorithm>
 #include <cmath>
@@ -56,8 +57,52 @@ static M2 mul(const M2& x, const M2& y) {
             x[2] * y[1] + x[3] * y[3]};
 }
 
+// adj_group_passes: every wire in exactly one pass; each tile at most max_bits bits of the
+// register, holding the pass's wires and bits 0..4; a run over all n wires takes
+// 1 + ceil((n - 11) / 6) passes from 12 qubits (one pass up to 11).
+static int check_group_passes(std::mt19937_64& rng) {
+    int fails = 0;
+    for (int n = 1; n <= 34; ++n)
+        for (int trial = 0; trial < 40; ++trial) {
+            std::vector<int> bits;
+            for (int b = 0; b < n; ++b)
+                if (trial == 0 || (rng() & 1)) bits.push_back(b);
+            std::shuffle(bits.begin(), bits.end(), rng);
+            const auto passes = qgpu::adj_group_passes(bits, n, qgpu::ADJ_GROUP_TILE_BITS);
+            std::vector<int> seen(bits.size(), 0);
+            for (const auto& p : passes) {
+                const uint64_t mask = p.first;
+                const int kmax = std::min(n, qgpu::ADJ_GROUP_TILE_BITS);
+                const uint64_t low = (1ull << std::min(n, 5)) - 1;
+                if (__builtin_popcountll(mask) > kmax || (mask & low) != low || (mask >> n) != 0 ||
+                    p.second.empty())
+                    ++fails;
+                for (size_t w : p.second) {
+                    if (w >= bits.size() || !((mask >> bits[w]) & 1ull)) ++fails;
+                    else ++seen[w];
+                }
+            }
+            for (int c : seen)
+                if (c != 1) ++fails;
+            if (trial == 0) {
+                const size_t want = n <= 11 ? 1 : 1 + (size_t)((n - 11 + 5) / 6);
+                if (passes.size() != want) {
+                    std::printf("n=%d: %zu passes, expected %zu\n", n, passes.size(), want);
+                    ++fails;
+                }
+            }
+        }
+    return fails;
+}
+
 int main() {
     int fails = 0;
+    {
+        std::mt19937_64 grng(19);
+        const int gf = check_group_passes(grng);
+        std::printf("group_passes fails %d\n", gf);
+        fails += gf;
+    }
     // inverse_op on every kind, 3 qubits: U^dag U = I through the tabulated images
     {
         const int n = 3;

@@ -1,9 +1,10 @@
 """The adjoint sweep's host-side algebra checked without a GPU (tests/cpp/adjoint_host.cpp):
 inverse_op against the library's own tabulation for every gate kind, and the Pauli-sum
 coefficients of single-wire runs (pauli_run, quantr_gb300/csrc/plan.cpp) against central
-differences of the energy (h = 1e-6; bar 1e-8, measured about 1e-9), and the gather tables of
+differences of the energy (h = 1e-6; bar 1e-8, measured about 1e-9), the gather tables of
 CNot / X / Swap runs (affine_tables, the k_linperm pass) against the gates applied one by one
-(exact)."""
+(exact), and the wire-to-pass partition of the grouped sweep (adj_group_passes: every wire once,
+tiles of at most 11 bits holding bits 0..4, the expected pass counts)."""
 import subprocess
 from pathlib import Path
 
