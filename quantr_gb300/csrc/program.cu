@@ -732,11 +732,18 @@ __global__ void __launch_bounds__(256) k_tile(typename P::S* __restrict__ st, co
 #pragma unroll
             for (int u = 0; u < U; ++u) P::real(v[u][0], v[u][1], p.steps[0]);
         } else if constexpr (ONE == ST_TABLE && IsArith<P>::value) {
-            // QFT rows: unconditional REAL / DENSE steps and phase tables only (no dispatch over
-            // the other step kinds, no control test on the 2x2 steps)
+            // QFT rows and rotation layers: unconditional REAL / DENSE steps, +-1/+-i monomials and
+            // phase tables only (no dispatch over the other step kinds, no control test on the
+            // 2x2 steps)
             for (int s = 0; s < p.nsteps; ++s) {
                 const DevStep& sp = p.steps[s];
-                if (sp.type == ST_TABLE) {
+                if (sp.type == ST_PERM) {  // +-1 / +-i monomial under its control mask
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        if (sp.lb == 0) step_on_bit<K, 0, P>(v[u], sp, base[u], off);
+                        if constexpr (K > 1) if (sp.lb == 1) step_on_bit<K, (K > 1 ? 1 : 0), P>(v[u], sp, base[u], off);
+                    }
+                } else if (sp.type == ST_TABLE) {
 #pragma unroll
                     for (int u = 0; u < U; ++u)
 #pragma unroll
@@ -1128,16 +1135,18 @@ static int launch_tile_t(qgpu_handle* h, const TileParams& p) {
         }
     }
     if constexpr ((K == 1 || K == 2) && IsArith<P>::value) {
-        // passes of unconditional 2x2 steps and phase tables only (the QFT rows): straight-line
-        // variant; tuning knob QGPU_TABLE_STRAIGHT=0 keeps the step loop
+        // passes of unconditional 2x2 steps, monomials and phase tables only (the QFT rows,
+        // rotation layers with their CNots): straight-line variant; tuning knob
+        // QGPU_TABLE_STRAIGHT=0 keeps the step loop
         static const int straight_tab = env_int("QGPU_TABLE_STRAIGHT", 1);
         bool ok = !launched && straight_tab != 0, any_table = false;
         for (int i = 0; i < p.nsteps && ok; ++i) {
             const DevStep& d = p.steps[i];
             any_table = any_table || d.type == ST_TABLE;
-            ok = d.type == ST_TABLE || ((d.type == ST_DENSE || d.type == ST_REAL) && d.cm == 0);
+            ok = d.type == ST_TABLE || d.type == ST_PERM ||
+                 ((d.type == ST_DENSE || d.type == ST_REAL) && d.cm == 0);
         }
-        if (ok && any_table) {
+        if (ok && (any_table || p.nsteps > 1)) {
             k_tile<K, U, P, ST_TABLE><<<(unsigned)blocks, 256, 0, h->stream>>>(s, p);
             launched = true;
         }
