@@ -3,7 +3,7 @@
 
 Workload (the metric's configuration): 20 brickwork layers of Rz(a) Ry(b) Rz(c) on every wire plus
 alternating CNot(i -> i+1) pairs, then a 30-qubit QFT (H + CRk(k) in quantr's examples/qft.rs
-pattern, then wire swaps): 2 580 gates on a 16 GiB complex128 state, seeded synthetic angles.
+pattern, then wire swaps): 2 570 gates on a 16 GiB complex128 state, seeded synthetic angles.
 
 A step = one `Circuit::simulate` of that circuit from |0...0> on a device-resident register
 (set_zero + qgpu_apply_program), timed with CUDA events on the library's stream. The 16 GiB state
